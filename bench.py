@@ -1,0 +1,447 @@
+#!/usr/bin/env python
+"""Benchmark: plain FP64 speculative segmented-sum SpMV on one GB300 (per rank).
+
+Workload (default ``powerlaw_4m``): m = n = 4,194,304, Zipf(2.1)-tailed row lengths
+clipped to [1, 200,000], 5 % empty rows, about 59 M non-zeros, values and x uniform[-1, 1]
+(seeded synthetic data, see benchmark_spmv_using_csr_gb300/gen.py).  One step = one
+y = A.x through the library (the tile kernel + the calibration kernel).
+
+Metric: SpMV HBM GB/s on the algorithmic bytes B = nnz*(s_val+4) + (m+1)*4 + n*s_x + m*s_y
+(val + col_idx + row_ptr + x + y, each counted once).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload powerlaw_4m|stencil27_160|stencil5_256] [--no-forms]
+
+* ``value``: B / (device time per step), inputs resident in HBM, L2 flushed (256 MiB
+  write) before every timed step, CUDA events on the launching stream, max over ranks.
+* ``e2e``: the same metric through the reference-facing C ABI with host buffers:
+  bhsp_set_x (x from pinned host memory), bhsp_run_benchmark, bhsp_get_y (y to pinned
+  host memory), all inside the timed region.
+* ``roofline``: the tile kernel alone (CUDA events between its launch and the
+  calibration launch) against the measured HBM copy bandwidth.
+* ``cpu_baseline``: the reference's serial CSR loop (spmv_cuda/main.cu:755-761, a port in
+  oracle/) on one host core over whole-matrix passes.
+* ``--impl reference``: the reference's OpenMP CSR loop (spmv_cuda/main.cu:377-393, same
+  port) on all host cores, same workload / metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "SpMV HBM GB/s (% of peak), mixed/batched vs plain FP64 at stated rel. error"
+UNIT = "GB/s"
+FALLBACK_HBM_GBS = 6800.0
+FLUSH_BYTES = 256 << 20
+
+WORKLOAD_TEXT = {
+    "powerlaw_4m": "power-law m=n=4,194,304: row lengths floor(1.98*U^(-1/1.1)) clipped to "
+                   "[1,200000] (Zipf 2.1 tail), 5% rows empty, distinct sorted uniform columns, "
+                   "val and x uniform[-1,1]; plain FP64 (USE_DOUBLE=1)",
+    "stencil27_160": "27-point stencil on a 160^3 grid, m=n=4,096,000, nnz=109,215,352, "
+                     "weights 26/-1 x (1+U[-0.01,0.01]), x uniform[-1,1]; plain FP64",
+    "stencil5_256": "5-point Laplacian on a 256^2 grid, m=n=65,536, nnz=326,656, values 4/-1 + "
+                    "U[-1e-3,1e-3], x uniform[-1,1]; plain FP64",
+}
+
+
+def alg_bytes(m: int, n: int, nnz: int, s_v: int, s_x: int, s_y: int, k: int = 1) -> int:
+    return nnz * (s_v + 4) + (m + 1) * 4 + n * k * s_x + m * k * s_y
+
+
+def reference_formula_bytes(m: int, nnz: int, s_v: int) -> int:
+    """spmv_cuda/main.cu:688 (counts x once per non-zero)."""
+    return (m + 1 + nnz) * 4 + (2 * nnz + m) * s_v
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(kernel_workload: str):
+    """Per-launch DRAM bytes of the tile kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"{kernel_workload}.txt")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch"):
+                return int(float(line.split("=")[1].split()[0]))
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
+
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.proc = None
+        self.out = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        rows = []
+        for line in out.splitlines():
+            f = [v.strip() for v in line.split(",")]
+            if len(f) < 10:
+                continue
+            if self.uuid and self.uuid not in f[0]:
+                continue
+            rows.append(f)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        loaded = [r for r in rows if (num(r[4]) or 0) > 0] or rows
+        sm = [num(r[1]) for r in loaded if num(r[1])]
+        reasons = set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in loaded:
+            for name, v in zip(names, r[6:10]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": num(loaded[0][2]), "samples": len(loaded),
+                "power_w_max": max((num(r[3]) or 0) for r in loaded), "reasons": sorted(reasons)}
+
+
+def make_workload(name: str):
+    from benchmark_spmv_using_csr_gb300 import gen
+    a = gen.WORKLOADS[name]()
+    x = gen.uniform(a.n, 7)
+    return a, x
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ---------------------------------------------------------------------------------------
+# reference arm: the reference's CPU path (port) on all host cores
+# ---------------------------------------------------------------------------------------
+def run_reference(args) -> None:
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    import oracle
+    a, x = make_workload(args.workload)
+    threads = os.cpu_count() or 1
+    B = alg_bytes(a.m, a.n, a.nnz, 8, 8, 8)
+    y = np.zeros(a.m)
+    for _ in range(args.warmup):
+        oracle.csr_omp(a.row_ptr, a.col, a.val, x, threads, y=y)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.csr_omp(a.row_ptr, a.col, a.val, x, threads, y=y)
+        ts.append(time.perf_counter() - t0)
+    sec = sum(ts)
+    value = B * args.steps / sec / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * sec / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "description": WORKLOAD_TEXT[args.workload],
+                   "m": a.m, "n": a.n, "nnz": a.nnz, "bytes_per_step": B},
+        "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads,
+                         "kind": "port",
+                         "sample": "whole matrix per step; OpenMP CSR loop of spmv_cuda/main.cu:"
+                                   "377-393 (C port in oracle/), all host threads; the reference's "
+                                   "own build (sm_32, CUDA-samples headers, removed cuSPARSE "
+                                   "calls) does not compile with CUDA 13"},
+        "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------------------
+def run_ours(args) -> None:
+    import numpy as np
+    import torch
+
+    import benchmark_spmv_using_csr_gb300 as sp
+    import oracle
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if not os.path.exists(sp.LIB_PATH):
+        sp.build()
+
+    a, x = make_workload(args.workload)
+    B = alg_bytes(a.m, a.n, a.nnz, 8, 8, 8)
+    seg, tpw, warps = args.config
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # pinned host buffers for x and y (the e2e leg reads / writes them every step)
+    x_pin = torch.from_numpy(x).pin_memory()
+    y_pin = torch.zeros(a.m, dtype=torch.float64).pin_memory()
+    y_np = y_pin.numpy()
+    h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    assert h.set_config(seg, tpw, warps) == 0, h.last_error
+    assert h.set_device(local) == 0
+    assert h.init_platform() == 0, h.last_error
+    t_prep = time.perf_counter()
+    rc = h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x_pin.numpy(), y_np)
+    assert rc == 0, h.last_error
+    t_prep = time.perf_counter() - t_prep
+
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+
+    def step_async():
+        assert h.run_phase(sptr, 3) == 0, h.last_error
+
+    # warm-up, then a short soak so that the clock sampler sees the GPU under this load
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step_async()
+    assert h.check() == 0, h.last_error
+    try:
+        uuid = str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        uuid = None
+    sampler = ClockSampler(uuid)
+    sampler.start()
+    t_end = time.perf_counter() + args.soak
+    with torch.cuda.stream(stream):
+        while time.perf_counter() < t_end:
+            for _ in range(20):
+                flush.fill_(1)
+                step_async()
+            stream.synchronize()
+
+    # timed region: exactly K steps, L2 flushed before each, events around both phases
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            e0, e1, e2 = ev[i]
+            e0.record(stream)
+            assert h.run_phase(sptr, 1) == 0, h.last_error
+            e1.record(stream)
+            assert h.run_phase(sptr, 2) == 0, h.last_error
+            e2.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    assert h.check() == 0, h.last_error
+    step_ms = [e0.elapsed_time(e2) for e0, _, e2 in ev]
+    kern_ms = [e0.elapsed_time(e1) for e0, e1, _ in ev]
+    cal_ms = [e1.elapsed_time(e2) for _, e1, e2 in ev]
+    total_s = sum(step_ms) / 1e3
+    if dist is not None:
+        t = torch.tensor([total_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * B * args.steps / total_s / 1e9
+
+    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    x_ptr = x_pin.data_ptr()
+    for _ in range(3):
+        assert h.set_x_ptr(x_ptr) == 0 and h.run_benchmark() == 0 and h.get_y() == 0
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        assert h.set_x_ptr(x_ptr) == 0, h.last_error
+        assert h.run_benchmark() == 0, h.last_error
+        assert h.get_y() == 0, h.last_error
+    e2e_s = time.perf_counter() - t0
+    barrier()
+    e2e_value = world * B * args.steps / e2e_s / 1e9
+
+    # correctness of the benchmarked y against the FP64 compensated oracle
+    ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)
+    scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, x)
+    rel_err = oracle.componentwise_error(y_np, ystar, scale)
+
+    line = None
+    if rank == 0:
+        peak, peak_kind = measured_peak()
+        kmean = statistics.mean(kern_ms)
+        achieved = B / (kmean * 1e-3) / 1e9
+        kw = f"k_tiles_f64_{args.workload}"
+        traffic = profile_traffic(kw)
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(statistics.mean(step_ms), 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generators; no dataset)",
+            "config": {"workload": args.workload, "description": WORKLOAD_TEXT[args.workload],
+                       "m": a.m, "n": a.n, "nnz": a.nnz, "bytes_per_step": B,
+                       "reference_formula_bytes": reference_formula_bytes(a.m, a.nnz, 8),
+                       "tile": {"nnz_per_lane": seg, "tiles_per_worker": tpw,
+                                "warps_per_cta": warps},
+                       "l2": "256 MiB flush write before every timed step; A (0.7 GB) > L2",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "pct_peak": round(100.0 * value / peak, 2),
+            "rel_error": {"componentwise_vs_fp64_dot2": rel_err, "tolerance": 1e-12},
+            "phases_ms": {"tile_kernel": round(kmean, 5),
+                          "calibration": round(statistics.mean(cal_ms), 5)},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": traffic, "peak_kind": f"{peak_kind} (hbm_gbs copy, burst)",
+                         "kernel": "k_tiles<PolF64> (tile kernel alone)"},
+            "e2e": {"value": round(e2e_value, 2), "unit": UNIT,
+                    "h2d_bytes_per_step": a.n * 8, "d2h_bytes_per_step": a.m * 8,
+                    "path": "bhsp_set_x + bhsp_run_benchmark + bhsp_get_y, pinned host x/y"},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clocks,
+            "prepare_mem_s": round(t_prep, 3),
+        }
+    h.free_mem()
+    h.close()
+
+    if rank == 0 and args.forms:
+        line["forms"] = measure_forms(args, a, x, ystar)
+    if rank == 0 and args.cpu_baseline > 0:
+        line["cpu_baseline"] = cpu_baseline(a, x, B, args.cpu_baseline)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def measure_forms(args, a, x, ystar) -> dict:
+    """The other value types on the same workload: device GB/s on their own algorithmic
+    bytes, non-zeros/s, and their error against the FP64 oracle."""
+    import numpy as np
+    import torch
+
+    import benchmark_spmv_using_csr_gb300 as sp
+    import oracle
+    out = {}
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    steps = max(10, min(args.steps, 50))
+    for vt, sv, sx in ((sp.VALUE_F32, 4, 4), (sp.VALUE_MIXED_F32, 4, 4), (sp.VALUE_MIXED_BF16, 2, 4)):
+        h = sp.BhsparseSpmvCuda(vt)
+        dt = sp.host_dtype(vt)
+        y = np.zeros(a.m, dt)
+        if h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val.astype(dt), x.astype(dt), y):
+            out[sp.VALUE_NAMES[vt]] = {"error": h.last_error}
+            continue
+        stream = torch.cuda.Stream()
+        with torch.cuda.stream(stream):
+            for _ in range(5):
+                h.run_phase(stream.cuda_stream, 3)
+            evs = []
+            for i in range(steps):
+                flush.fill_(i & 0xFF)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                h.run_phase(stream.cuda_stream, 3)
+                e1.record(stream)
+                evs.append((e0, e1))
+        torch.cuda.synchronize()
+        assert h.check() == 0, h.last_error
+        ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in evs)
+        assert h.get_y() == 0
+        Bf = alg_bytes(a.m, a.n, a.nnz, sv, sx, 4)
+        out[sp.VALUE_NAMES[vt]] = {
+            "gbs": round(Bf / (ms * 1e-3) / 1e9, 1), "ms_per_step": round(ms, 5),
+            "gnnz_per_s": round(a.nnz / (ms * 1e-3) / 1e9, 2),
+            "normwise_err_vs_fp64_oracle": oracle.normwise_error(y, ystar)}
+        h.close()
+    return out
+
+
+def cpu_baseline(a, x, B, seconds: float) -> dict:
+    """The reference's serial CSR loop (spmv_cuda/main.cu:755-761, C port) on one host core,
+    whole-matrix passes until `seconds` have elapsed."""
+    import numpy as np
+    import oracle
+    y = np.zeros(a.m)
+    passes = 0
+    t0 = time.perf_counter()
+    while True:
+        oracle.csr_serial_rows(a.row_ptr, a.col, a.val, x, y, 0, a.m)
+        passes += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return {"value": round(B * passes / el / 1e9, 3), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{passes} whole-matrix passes of the serial CSR loop (spmv_cuda/main.cu:"
+                      f"755-761, C port in oracle/) in {el:.1f} s on one host core"}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", choices=tuple(WORKLOAD_TEXT), default="powerlaw_4m")
+    ap.add_argument("--config", type=int, nargs=3, default=(32, 4, 8),
+                    metavar=("NNZ_PER_LANE", "TILES_PER_WORKER", "WARPS_PER_CTA"))
+    ap.add_argument("--soak", type=float, default=1.5, help="seconds of untimed steps for clocks")
+    ap.add_argument("--cpu-baseline", type=float, default=10.0,
+                    help="seconds of serial CPU baseline (0 = skip)")
+    ap.add_argument("--no-forms", dest="forms", action="store_false")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,97 @@
+"""ctypes binding of ``libspmv_gb300.so`` (the C ABI of include/spmv_gb300.h and
+include/spmv_gen.h).
+
+The library is built in-tree by :mod:`benchmark_spmv_using_csr_gb300.build`.  If it
+is missing this module raises at load time: there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from .build import LIB_PATH
+
+_lock = threading.Lock()
+_lib = None
+
+c_int, c_int64, c_uint64, c_size_t, c_double = (ctypes.c_int, ctypes.c_int64, ctypes.c_uint64,
+                                                 ctypes.c_size_t, ctypes.c_double)
+c_void_p, c_char_p = ctypes.c_void_p, ctypes.c_char_p
+P_int = ctypes.POINTER(ctypes.c_int)
+P_void = ctypes.POINTER(ctypes.c_void_p)
+
+# name -> (restype, argtypes); every entry is a symbol declared in include/*.h
+SIGNATURES = {
+    # handle API (spmv_gb300.h)
+    "bhsp_create": (c_int, [P_void, c_int]),
+    "bhsp_destroy": (None, [c_void_p]),
+    "bhsp_init_platform": (c_int, [c_void_p]),
+    "bhsp_free_platform": (c_int, [c_void_p]),
+    "bhsp_prepare_mem": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_void_p]),
+    "bhsp_run_benchmark": (c_int, [c_void_p]),
+    "bhsp_get_y": (c_int, [c_void_p]),
+    "bhsp_free_mem": (c_int, [c_void_p]),
+    "bhsp_last_error": (c_char_p, [c_void_p]),
+    "bhsp_set_device": (c_int, [c_void_p, c_int]),
+    "bhsp_set_config": (c_int, [c_void_p, c_int, c_int, c_int]),
+    "bhsp_get_config": (c_int, [c_void_p, P_int, P_int, P_int]),
+    "bhsp_set_x": (c_int, [c_void_p, c_void_p]),
+    "bhsp_run_async": (c_int, [c_void_p, c_void_p]),
+    "bhsp_check": (c_int, [c_void_p]),
+    "bhsp_run_phase": (c_int, [c_void_p, c_void_p, c_int]),
+    "bhsp_device_buffers": (c_int, [c_void_p, P_void, P_void, P_void, P_void, P_void]),
+    "bhsp_device_bytes": (c_size_t, [c_void_p]),
+    # plan API
+    "bhsp_plan_create": (c_int, [P_void, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int,
+                                 c_int, c_int, c_void_p]),
+    "bhsp_plan_execute": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "bhsp_plan_execute_phase": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
+    "bhsp_plan_check": (c_int, [c_void_p, c_void_p]),
+    "bhsp_plan_launches": (c_int, [c_void_p]),
+    "bhsp_plan_tiles": (c_int, [c_void_p, P_void, P_int, P_int]),
+    "bhsp_plan_last_error": (c_char_p, [c_void_p]),
+    "bhsp_plan_destroy": (None, [c_void_p]),
+    # partition primitives
+    "bhsp_partition": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p]),
+    "bhsp_bitflags": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "bhsp_validate_csr": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p]),
+    "bhsp_version": (c_char_p, []),
+    # generators (spmv_gen.h)
+    "bhsp_gen_uniform": (c_int, [c_int64, c_uint64, c_double, c_double, c_void_p]),
+    "bhsp_gen_uniform_int": (c_int, [c_int64, c_uint64, c_int, c_void_p]),
+    "bhsp_gen_stencil2d_nnz": (c_int64, [c_int, c_int]),
+    "bhsp_gen_stencil2d": (c_int, [c_int, c_int, c_double, c_uint64, c_void_p, c_void_p, c_void_p]),
+    "bhsp_gen_stencil3d_nnz": (c_int64, [c_int, c_int, c_int]),
+    "bhsp_gen_stencil3d": (c_int, [c_int, c_int, c_int, c_double, c_uint64, c_void_p, c_void_p,
+                                   c_void_p]),
+    "bhsp_gen_powerlaw_rows": (c_int64, [c_int, c_double, c_double, c_int, c_double, c_uint64,
+                                         c_void_p]),
+    "bhsp_gen_density_rows": (c_int64, [c_int, c_int, c_double, c_uint64, c_void_p]),
+    "bhsp_gen_mixed_rows": (c_int64, [c_int, c_int, c_int, c_double, c_double, c_uint64,
+                                      c_void_p]),
+    "bhsp_gen_random_fill": (c_int, [c_int, c_int, c_void_p, c_double, c_double, c_uint64,
+                                     c_void_p, c_void_p]),
+    "bhsp_gen_blockdiag_rows": (c_int64, [c_int, c_int, c_int, c_void_p]),
+    "bhsp_gen_blockdiag_fill": (c_int, [c_int, c_int, c_int, c_double, c_double, c_uint64,
+                                        c_void_p, c_void_p, c_void_p]),
+}
+
+
+def lib() -> ctypes.CDLL:
+    """Load the library (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"{LIB_PATH} is missing: build it with "
+                    "`python -m benchmark_spmv_using_csr_gb300.build` (no fallback path exists)")
+            L = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+        return _lib

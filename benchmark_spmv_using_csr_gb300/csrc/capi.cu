@@ -1,0 +1,573 @@
+// capi.cu -- the C ABI (include/spmv_gb300.h): handle API mirroring bhsparse_spmv_cuda
+// (spmv_cuda/bhsparse_spmv_cuda.h:7-351) and the device-pointer plan API.
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/spmv_gb300.h"
+#include "internal.h"
+
+using namespace spmv;
+
+namespace {
+
+constexpr int kDefaultSeg = 32;
+constexpr int kDefaultTpw = 4;
+constexpr int kDefaultWarps = 8;
+
+bool valid_vt(int vt) { return vt >= BHSP_VALUE_F64 && vt <= BHSP_VALUE_MIXED_BF16; }
+bool supported_vt(int vt) { return is_supported_value_type(vt); }
+
+// bytes of one stored matrix value / one x or y entry on the device
+size_t val_bytes(int vt) {
+    switch (vt) {
+        case BHSP_VALUE_F64: return 8;
+        case BHSP_VALUE_F32: return 4;
+        case BHSP_VALUE_MIXED_F32: return 4;
+        default: return 2;
+    }
+}
+size_t vec_bytes(int vt) { return vt == BHSP_VALUE_F64 ? 8 : 4; }
+// bytes of one value as the host passes it through the handle API
+size_t host_bytes(int vt) { return vt == BHSP_VALUE_F32 ? 4 : 8; }
+
+bool config_ok(const TileConfig& c) {
+    return (c.seg == 8 || c.seg == 16 || c.seg == 32) && c.tiles_per_worker >= 1 &&
+           c.tiles_per_worker <= (1 << 20) && (c.warps_per_cta == 4 || c.warps_per_cta == 8);
+}
+
+TileConfig make_config(int seg, int tpw, int warps) {
+    TileConfig c;
+    c.seg = seg > 0 ? seg : kDefaultSeg;
+    c.tiles_per_worker = tpw > 0 ? tpw : kDefaultTpw;
+    c.warps_per_cta = warps > 0 ? warps : kDefaultWarps;
+    return c;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------------------
+// Plan
+// ----------------------------------------------------------------------------------------
+struct bhsp_plan {
+    int vt = 0, m = 0, n = 0, nnz = 0;
+    TileConfig cfg{};
+    int ntiles = 0, nworkers = 0;
+    const int* row_ptr = nullptr;
+    const int* col = nullptr;
+    uint32_t* tile_ptr = nullptr;
+    int* rec_row = nullptr;
+    void* rec_val = nullptr;
+    uint32_t* err = nullptr;  // device error word
+    int device = 0;
+    std::string last_error;
+};
+
+static int plan_fail(bhsp_plan* p, int code, const std::string& msg) {
+    if (p) p->last_error = msg;
+    return code;
+}
+
+static int cuda_fail(std::string* sink, cudaError_t e, const char* what) {
+    if (sink) *sink = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? BHSPARSE_OUT_OF_MEMORY : BHSPARSE_CUDA_ERROR;
+}
+
+#define PLAN_CUDA(p, call)                                               \
+    do {                                                                 \
+        cudaError_t e_ = (call);                                         \
+        if (e_ != cudaSuccess) return cuda_fail(&(p)->last_error, e_, #call); \
+    } while (0)
+
+static void plan_release(bhsp_plan* p) {
+    if (!p) return;
+    cudaFree(p->tile_ptr);
+    cudaFree(p->rec_row);
+    cudaFree(p->rec_val);
+    cudaFree(p->err);
+    p->tile_ptr = nullptr;
+    p->rec_row = nullptr;
+    p->rec_val = nullptr;
+    p->err = nullptr;
+}
+
+static int validate_on_device(const int* row_ptr, const int* col, int m, int n, int nnz,
+                              cudaStream_t st, std::string* sink) {
+    uint32_t* bad = nullptr;
+    cudaError_t e = cudaMalloc(&bad, sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_fail(sink, e, "cudaMalloc(validate)");
+    uint32_t h = 0;
+    e = cudaMemsetAsync(bad, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = launch_validate(row_ptr, col, m, n, nnz, bad, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, bad, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(bad);
+    if (e != cudaSuccess) return cuda_fail(sink, e, "CSR validation");
+    if (h) {
+        if (sink)
+            *sink = (h & 1u) ? "invalid CSR: row_ptr must start at 0, be non-decreasing and end at nnz"
+                             : "invalid CSR: a column index lies outside [0, n)";
+        return BHSPARSE_INVALID_CSR;
+    }
+    return BHSPARSE_SUCCESS;
+}
+
+static int check_sizes(int m, int n, int nnz, std::string* sink) {
+    if (m < 0 || n < 0 || nnz < 0 || nnz > BHSP_MAX_NNZ) {
+        if (sink) *sink = "sizes must satisfy m >= 0, n >= 0, 0 <= nnz <= BHSP_MAX_NNZ";
+        return BHSPARSE_INVALID_ARGUMENT;
+    }
+    if (nnz > 0 && n == 0) {
+        if (sink) *sink = "nnz > 0 needs n > 0";
+        return BHSPARSE_INVALID_ARGUMENT;
+    }
+    return BHSPARSE_SUCCESS;
+}
+
+static int plan_build(bhsp_plan* p, cudaStream_t st) {
+    const int tile = 32 * p->cfg.seg;
+    p->ntiles = num_tiles(p->nnz, tile);
+    p->nworkers = (p->ntiles + p->cfg.tiles_per_worker - 1) / p->cfg.tiles_per_worker;
+    PLAN_CUDA(p, cudaGetDevice(&p->device));
+    PLAN_CUDA(p, cudaMalloc(&p->tile_ptr, sizeof(uint32_t) * (p->ntiles + 1)));
+    PLAN_CUDA(p, cudaMalloc(&p->rec_row, sizeof(int) * (p->nworkers > 0 ? p->nworkers : 1)));
+    PLAN_CUDA(p, cudaMalloc(&p->rec_val, 8 * (size_t)(p->nworkers > 0 ? p->nworkers : 1)));
+    PLAN_CUDA(p, cudaMalloc(&p->err, sizeof(uint32_t)));
+    PLAN_CUDA(p, cudaMemsetAsync(p->err, 0, sizeof(uint32_t), st));
+    PLAN_CUDA(p, launch_partition(p->row_ptr, p->m, p->nnz, tile, p->tile_ptr, st));
+    return BHSPARSE_SUCCESS;
+}
+
+static int plan_execute(bhsp_plan* p, const void* val, const void* x, void* y, cudaStream_t st,
+                        int phase = 3) {
+    if (p->m == 0) return BHSPARSE_SUCCESS;
+    cudaError_t e = cudaSuccess;
+    switch (p->vt) {
+        case BHSP_VALUE_F64:
+        case BHSP_VALUE_F32: {
+            PlainLaunch a;
+            a.row_ptr = p->row_ptr;
+            a.col = p->col;
+            a.val = val;
+            a.x = x;
+            a.y = y;
+            a.tile_ptr = p->tile_ptr;
+            a.rec_row = p->rec_row;
+            a.rec_val = p->rec_val;
+            a.err = p->err;
+            a.m = p->m;
+            a.n = p->n;
+            a.nnz = p->nnz;
+            a.phase = phase;
+            e = p->vt == BHSP_VALUE_F64 ? launch_plain_f64(a, p->cfg, st) : launch_plain_f32(a, p->cfg, st);
+            break;
+        }
+        default: {
+            MixedLaunch a;
+            a.row_ptr = p->row_ptr;
+            a.col = p->col;
+            a.val = val;
+            a.x = static_cast<const float*>(x);
+            a.y = static_cast<float*>(y);
+            a.tile_ptr = p->tile_ptr;
+            a.rec_row = p->rec_row;
+            a.rec_val = static_cast<double*>(p->rec_val);
+            a.err = p->err;
+            a.m = p->m;
+            a.n = p->n;
+            a.nnz = p->nnz;
+            a.bf16 = p->vt == BHSP_VALUE_MIXED_BF16;
+            a.phase = phase;
+            e = launch_mixed(a, p->cfg, st);
+            break;
+        }
+    }
+    if (e != cudaSuccess) return cuda_fail(&p->last_error, e, "SpMV launch");
+    return BHSPARSE_SUCCESS;
+}
+
+static int plan_check(bhsp_plan* p, cudaStream_t st) {
+    uint32_t h = 0;
+    PLAN_CUDA(p, cudaMemcpyAsync(&h, p->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    PLAN_CUDA(p, cudaStreamSynchronize(st));
+    if (h) {
+        PLAN_CUDA(p, cudaMemsetAsync(p->err, 0, sizeof(uint32_t), st));
+        PLAN_CUDA(p, cudaStreamSynchronize(st));
+        char buf[96];
+        snprintf(buf, sizeof buf, "device-side check failed (error word 0x%x)", h);
+        return plan_fail(p, BHSPARSE_DEVICE_CHECK_FAILED, buf);
+    }
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_plan_create(bhsp_plan** out, int value_type, int m, int n, int nnz,
+                                const int* d_row_ptr, const int* d_col_idx, int seg,
+                                int tiles_per_worker, int warps_per_cta, void* stream) {
+    if (!out) return BHSPARSE_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (!valid_vt(value_type) || !supported_vt(value_type)) return BHSPARSE_UNSUPPORTED_VALUE_TYPE;
+    std::string msg;
+    int rc = check_sizes(m, n, nnz, &msg);
+    if (rc) return rc;
+    if (!d_row_ptr || (nnz > 0 && !d_col_idx)) return BHSPARSE_INVALID_ARGUMENT;
+    TileConfig cfg = make_config(seg, tiles_per_worker, warps_per_cta);
+    if (!config_ok(cfg)) return BHSPARSE_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    rc = validate_on_device(d_row_ptr, d_col_idx, m, n, nnz, st, &msg);
+    if (rc) return rc;
+    bhsp_plan* p = new bhsp_plan;
+    p->vt = value_type;
+    p->m = m;
+    p->n = n;
+    p->nnz = nnz;
+    p->cfg = cfg;
+    p->row_ptr = d_row_ptr;
+    p->col = d_col_idx;
+    rc = plan_build(p, st);
+    if (rc) {
+        plan_release(p);
+        delete p;
+        return rc;
+    }
+    *out = p;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_plan_execute(bhsp_plan* p, const void* d_val, const void* d_x, void* d_y,
+                                 void* stream) {
+    if (!p) return BHSPARSE_INVALID_ARGUMENT;
+    if (p->m > 0 && (!d_y || (p->nnz > 0 && (!d_val || !d_x))))
+        return plan_fail(p, BHSPARSE_INVALID_ARGUMENT, "null device buffer");
+    return plan_execute(p, d_val, d_x, d_y, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int bhsp_plan_execute_phase(bhsp_plan* p, const void* d_val, const void* d_x,
+                                       void* d_y, void* stream, int phase) {
+    if (!p || phase < 1 || phase > 3) return BHSPARSE_INVALID_ARGUMENT;
+    if (p->m > 0 && (!d_y || (p->nnz > 0 && (!d_val || !d_x))))
+        return plan_fail(p, BHSPARSE_INVALID_ARGUMENT, "null device buffer");
+    return plan_execute(p, d_val, d_x, d_y, static_cast<cudaStream_t>(stream), phase);
+}
+
+extern "C" int bhsp_plan_check(bhsp_plan* p, void* stream) {
+    if (!p) return BHSPARSE_INVALID_ARGUMENT;
+    return plan_check(p, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int bhsp_plan_launches(const bhsp_plan* p) {
+    if (!p) return 0;
+    return p->m == 0 ? 0 : (p->nworkers > 0 ? 2 : 1);
+}
+
+extern "C" int bhsp_plan_tiles(const bhsp_plan* p, const uint32_t** d_tile_ptr, int* ntiles,
+                               int* tile_nnz) {
+    if (!p) return BHSPARSE_INVALID_ARGUMENT;
+    if (d_tile_ptr) *d_tile_ptr = p->tile_ptr;
+    if (ntiles) *ntiles = p->ntiles;
+    if (tile_nnz) *tile_nnz = 32 * p->cfg.seg;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" const char* bhsp_plan_last_error(const bhsp_plan* p) {
+    return p ? p->last_error.c_str() : "null plan";
+}
+
+extern "C" void bhsp_plan_destroy(bhsp_plan* p) {
+    if (!p) return;
+    plan_release(p);
+    delete p;
+}
+
+// ----------------------------------------------------------------------------------------
+// Partition primitives
+// ----------------------------------------------------------------------------------------
+extern "C" int bhsp_partition(const int* d_row_ptr, int m, int nnz, int tile_nnz,
+                              uint32_t* d_tile_ptr, void* stream) {
+    if (check_sizes(m, 1, nnz, nullptr) || !d_row_ptr || !d_tile_ptr || tile_nnz < 1 ||
+        tile_nnz > 4096)
+        return BHSPARSE_INVALID_ARGUMENT;
+    cudaError_t e = launch_partition(d_row_ptr, m, nnz, tile_nnz, d_tile_ptr,
+                                     static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? BHSPARSE_SUCCESS : BHSPARSE_CUDA_ERROR;
+}
+
+extern "C" int bhsp_bitflags(const int* d_row_ptr, int m, int nnz, int seg,
+                             const uint32_t* d_tile_ptr, uint32_t* d_words, void* stream) {
+    if (check_sizes(m, 1, nnz, nullptr) || !d_row_ptr || !d_tile_ptr || (nnz > 0 && !d_words))
+        return BHSPARSE_INVALID_ARGUMENT;
+    if (seg != 1 && seg != 2 && seg != 4 && seg != 8 && seg != 16 && seg != 32)
+        return BHSPARSE_INVALID_ARGUMENT;
+    cudaError_t e = launch_bitflags(d_row_ptr, m, nnz, seg, d_tile_ptr, d_words,
+                                    static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? BHSPARSE_SUCCESS : BHSPARSE_CUDA_ERROR;
+}
+
+extern "C" int bhsp_validate_csr(const int* d_row_ptr, const int* d_col_idx, int m, int n, int nnz,
+                                 void* stream) {
+    int rc = check_sizes(m, n, nnz, nullptr);
+    if (rc) return rc;
+    if (!d_row_ptr || (nnz > 0 && !d_col_idx)) return BHSPARSE_INVALID_ARGUMENT;
+    return validate_on_device(d_row_ptr, d_col_idx, m, n, nnz, static_cast<cudaStream_t>(stream),
+                              nullptr);
+}
+
+extern "C" const char* bhsp_version(void) { return "gb300-spmv 1.0 (sm_103a)"; }
+
+// ----------------------------------------------------------------------------------------
+// Handle: the reference class bhsparse_spmv_cuda
+// ----------------------------------------------------------------------------------------
+struct bhsp_spmv {
+    int vt = BHSP_VALUE_F64;
+    int device = 0;
+    bool platform = false;
+    bool prepared = false;
+    TileConfig cfg = make_config(0, 0, 0);
+    int m = 0, n = 0, nnz = 0;
+    int* d_row_ptr = nullptr;
+    int* d_col = nullptr;
+    void* d_val = nullptr;   // storage type
+    void* d_x = nullptr;     // vector type
+    void* d_y = nullptr;     // vector type
+    double* d_stage = nullptr;  // FP64 staging for the mixed forms (max(m, n, nnz) entries)
+    void* h_y = nullptr;     // caller's y (get_y target)
+    bhsp_plan* plan = nullptr;
+    cudaStream_t stream = nullptr;  // stream used by run_benchmark / set_x / get_y
+    std::string last_error;
+    std::string device_name;
+};
+
+static int h_fail(bhsp_spmv* h, int code, const std::string& msg) {
+    h->last_error = msg;
+    return code;
+}
+
+#define H_CUDA(h, call)                                                   \
+    do {                                                                  \
+        cudaError_t e_ = (call);                                          \
+        if (e_ != cudaSuccess) return cuda_fail(&(h)->last_error, e_, #call); \
+    } while (0)
+
+extern "C" int bhsp_create(bhsp_spmv** out, int value_type) {
+    if (!out) return BHSPARSE_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (!valid_vt(value_type) || !supported_vt(value_type)) return BHSPARSE_UNSUPPORTED_VALUE_TYPE;
+    bhsp_spmv* h = new bhsp_spmv;
+    h->vt = value_type;
+    *out = h;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_set_device(bhsp_spmv* h, int device) {
+    if (!h || device < 0) return BHSPARSE_INVALID_ARGUMENT;
+    if (h->prepared) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "set_device after prepare_mem");
+    h->device = device;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_init_platform(bhsp_spmv* h) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    H_CUDA(h, cudaSetDevice(h->device));
+    cudaDeviceProp prop;
+    H_CUDA(h, cudaGetDeviceProperties(&prop, h->device));
+    h->device_name = prop.name;
+    h->platform = true;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_free_platform(bhsp_spmv* h) { return h ? BHSPARSE_SUCCESS : BHSPARSE_INVALID_ARGUMENT; }
+
+extern "C" int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int warps_per_cta) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (h->prepared) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "set_config after prepare_mem");
+    TileConfig c = make_config(seg, tiles_per_worker, warps_per_cta);
+    if (!config_ok(c)) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "unsupported tile config");
+    h->cfg = c;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tpw, int* warps) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (seg) *seg = h->cfg.seg;
+    if (tpw) *tpw = h->cfg.tiles_per_worker;
+    if (warps) *warps = h->cfg.warps_per_cta;
+    return BHSPARSE_SUCCESS;
+}
+
+static void handle_release(bhsp_spmv* h) {
+    if (h->plan) bhsp_plan_destroy(h->plan);
+    h->plan = nullptr;
+    cudaFree(h->d_row_ptr);
+    cudaFree(h->d_col);
+    cudaFree(h->d_val);
+    cudaFree(h->d_x);
+    cudaFree(h->d_y);
+    cudaFree(h->d_stage);
+    h->d_row_ptr = nullptr;
+    h->d_col = nullptr;
+    h->d_val = nullptr;
+    h->d_x = nullptr;
+    h->d_y = nullptr;
+    h->d_stage = nullptr;
+    h->prepared = false;
+}
+
+// host -> device copy of a value array, converting for the mixed forms
+static int upload_values(bhsp_spmv* h, void* dst, const void* src, size_t count, bool is_matrix) {
+    if (count == 0) return BHSPARSE_SUCCESS;
+    if (h->vt == BHSP_VALUE_F64 || h->vt == BHSP_VALUE_F32) {
+        H_CUDA(h, cudaMemcpyAsync(dst, src, count * host_bytes(h->vt), cudaMemcpyHostToDevice,
+                                  h->stream));
+        return BHSPARSE_SUCCESS;
+    }
+    H_CUDA(h, cudaMemcpyAsync(h->d_stage, src, count * 8, cudaMemcpyHostToDevice, h->stream));
+    const bool to_bf16 = is_matrix && h->vt == BHSP_VALUE_MIXED_BF16;
+    H_CUDA(h, launch_convert_from_f64(h->d_stage, dst, count, to_bf16, h->stream));
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_prepare_mem(bhsp_spmv* h, int m, int n, int nnz, const int* row_ptr,
+                                const int* col_idx, const void* val, const void* x, void* y) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    int rc = check_sizes(m, n, nnz, &h->last_error);
+    if (rc) return rc;
+    if (!row_ptr || (nnz > 0 && (!col_idx || !val)) || (n > 0 && !x) || (m > 0 && !y))
+        return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "null host array");
+    if (h->prepared) handle_release(h);
+    if (!h->platform) {
+        rc = bhsp_init_platform(h);
+        if (rc) return rc;
+    }
+    H_CUDA(h, cudaSetDevice(h->device));
+    h->m = m;
+    h->n = n;
+    h->nnz = nnz;
+    h->h_y = y;
+    const size_t vb = vec_bytes(h->vt);
+    H_CUDA(h, cudaMalloc(&h->d_row_ptr, sizeof(int) * ((size_t)m + 1)));
+    H_CUDA(h, cudaMalloc(&h->d_col, sizeof(int) * (size_t)(nnz > 0 ? nnz : 1)));
+    H_CUDA(h, cudaMalloc(&h->d_val, val_bytes(h->vt) * (size_t)(nnz > 0 ? nnz : 1) + 32));
+    H_CUDA(h, cudaMalloc(&h->d_x, vb * (size_t)(n > 0 ? n : 1)));
+    H_CUDA(h, cudaMalloc(&h->d_y, vb * (size_t)(m > 0 ? m : 1)));
+    if (h->vt >= BHSP_VALUE_MIXED_F32) {
+        size_t big = (size_t)m;
+        if ((size_t)n > big) big = n;
+        if ((size_t)nnz > big) big = nnz;
+        H_CUDA(h, cudaMalloc(&h->d_stage, 8 * (big > 0 ? big : 1)));
+    }
+    H_CUDA(h, cudaMemcpyAsync(h->d_row_ptr, row_ptr, sizeof(int) * ((size_t)m + 1),
+                              cudaMemcpyHostToDevice, h->stream));
+    if (nnz > 0)
+        H_CUDA(h, cudaMemcpyAsync(h->d_col, col_idx, sizeof(int) * (size_t)nnz,
+                                  cudaMemcpyHostToDevice, h->stream));
+    rc = upload_values(h, h->d_val, val, (size_t)nnz, true);
+    if (rc) return rc;
+    rc = upload_values(h, h->d_x, x, (size_t)n, false);
+    if (rc) return rc;
+    rc = upload_values(h, h->d_y, y, (size_t)m, false);
+    if (rc) return rc;
+    bhsp_plan* p = nullptr;
+    rc = bhsp_plan_create(&p, h->vt, m, n, nnz, h->d_row_ptr, h->d_col, h->cfg.seg,
+                          h->cfg.tiles_per_worker, h->cfg.warps_per_cta, h->stream);
+    if (rc) {
+        handle_release(h);
+        h->last_error = rc == BHSPARSE_INVALID_CSR ? "invalid CSR (row_ptr or col_idx)" : "plan creation failed";
+        return rc;
+    }
+    h->plan = p;
+    H_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->prepared = true;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_set_x(bhsp_spmv* h, const void* x) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (!h->prepared) return h_fail(h, BHSPARSE_NOT_PREPARED, "set_x before prepare_mem");
+    if (h->n > 0 && !x) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "null x");
+    return upload_values(h, h->d_x, x, (size_t)h->n, false);
+}
+
+extern "C" int bhsp_run_async(bhsp_spmv* h, void* stream) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (!h->prepared) return h_fail(h, BHSPARSE_NOT_PREPARED, "run before prepare_mem");
+    int rc = bhsp_plan_execute(h->plan, h->d_val, h->d_x, h->d_y, stream);
+    if (rc) h->last_error = h->plan->last_error;
+    return rc;
+}
+
+extern "C" int bhsp_run_phase(bhsp_spmv* h, void* stream, int phase) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (!h->prepared) return h_fail(h, BHSPARSE_NOT_PREPARED, "run before prepare_mem");
+    int rc = bhsp_plan_execute_phase(h->plan, h->d_val, h->d_x, h->d_y, stream, phase);
+    if (rc) h->last_error = h->plan->last_error;
+    return rc;
+}
+
+extern "C" int bhsp_check(bhsp_spmv* h) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (!h->prepared) return h_fail(h, BHSPARSE_NOT_PREPARED, "check before prepare_mem");
+    int rc = plan_check(h->plan, h->stream);
+    if (rc) h->last_error = h->plan->last_error;
+    return rc;
+}
+
+extern "C" int bhsp_run_benchmark(bhsp_spmv* h) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    int rc = bhsp_run_async(h, h->stream);
+    if (rc) return rc;
+    return bhsp_check(h);
+}
+
+extern "C" int bhsp_get_y(bhsp_spmv* h) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (!h->prepared) return h_fail(h, BHSPARSE_NOT_PREPARED, "get_y before prepare_mem");
+    if (h->m == 0) return BHSPARSE_SUCCESS;
+    if (h->vt == BHSP_VALUE_F64 || h->vt == BHSP_VALUE_F32) {
+        H_CUDA(h, cudaMemcpyAsync(h->h_y, h->d_y, (size_t)h->m * vec_bytes(h->vt),
+                                  cudaMemcpyDeviceToHost, h->stream));
+    } else {
+        H_CUDA(h, launch_convert_to_f64(static_cast<const float*>(h->d_y), h->d_stage, (size_t)h->m,
+                                        h->stream));
+        H_CUDA(h, cudaMemcpyAsync(h->h_y, h->d_stage, (size_t)h->m * 8, cudaMemcpyDeviceToHost,
+                                  h->stream));
+    }
+    H_CUDA(h, cudaStreamSynchronize(h->stream));
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_free_mem(bhsp_spmv* h) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (h->prepared) H_CUDA(h, cudaStreamSynchronize(h->stream));
+    handle_release(h);
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" void bhsp_destroy(bhsp_spmv* h) {
+    if (!h) return;
+    if (h->prepared) cudaStreamSynchronize(h->stream);
+    handle_release(h);
+    delete h;
+}
+
+extern "C" const char* bhsp_last_error(const bhsp_spmv* h) {
+    return h ? h->last_error.c_str() : "null handle";
+}
+
+extern "C" int bhsp_device_buffers(const bhsp_spmv* h, const int** row_ptr, const int** col_idx,
+                                   const void** val, void** x, void** y) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (!h->prepared) return BHSPARSE_NOT_PREPARED;
+    if (row_ptr) *row_ptr = h->d_row_ptr;
+    if (col_idx) *col_idx = h->d_col;
+    if (val) *val = h->d_val;
+    if (x) *x = h->d_x;
+    if (y) *y = h->d_y;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" size_t bhsp_device_bytes(const bhsp_spmv* h) {
+    if (!h || !h->prepared) return 0;
+    size_t b = sizeof(int) * ((size_t)h->m + 1) + sizeof(int) * (size_t)h->nnz +
+               val_bytes(h->vt) * (size_t)h->nnz + vec_bytes(h->vt) * ((size_t)h->n + h->m);
+    if (h->plan) b += sizeof(uint32_t) * ((size_t)h->plan->ntiles + 1) + 12 * (size_t)h->plan->nworkers;
+    return b;
+}

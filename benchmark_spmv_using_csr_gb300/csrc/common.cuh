@@ -1,0 +1,96 @@
+// common.cuh -- shared device helpers for the GB300 speculative segmented-sum SpMV.
+//
+// Streaming loads use 256-bit vector loads (ld.global.v4.f64 / v8.b32, sm_100+) with an
+// L2 evict-first policy, so that the val / col_idx stream does not push x out of L2;
+// x is gathered through the read-only path (ld.global.nc) with an L2 evict-last policy.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#define SPMV_FULL_MASK 0xffffffffu
+
+namespace spmv {
+
+// Error word bits set by kernels (read back by the host; no __trap anywhere).
+enum : uint32_t {
+    ERR_NONE = 0,
+    ERR_BAD_TILE = 1u << 0,      // a tile row span that cannot come from a valid row_ptr
+    ERR_LIST_OVERFLOW = 1u << 1, // more non-empty rows in a dirty tile span than fit in shared memory
+    ERR_QUEUE = 1u << 2,         // batched work queue gave out an index out of range
+};
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// ---- 256-bit streaming loads (address must be 32-byte aligned) ----
+__device__ __forceinline__ void ld_stream_f64x4(const double* p, uint64_t pol, double (&v)[4]) {
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f64 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3])
+                 : "l"(p), "l"(pol));
+}
+__device__ __forceinline__ void ld_stream_b32x8(const void* p, uint64_t pol, uint32_t (&v)[8]) {
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                   "=r"(v[7])
+                 : "l"(p), "l"(pol));
+}
+// 128-bit streaming load (16-byte aligned)
+__device__ __forceinline__ void ld_stream_b32x4(const void* p, uint64_t pol, uint32_t (&v)[4]) {
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.b32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+                 : "l"(p), "l"(pol));
+}
+
+// ---- x gathers: read-only path, kept in L2 ----
+__device__ __forceinline__ double ld_x(const double* p, uint64_t pol) {
+    double v;
+    asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float ld_x(const float* p, uint64_t pol) {
+    float v;
+    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+// ---- warp helpers ----
+template <typename T>
+__device__ __forceinline__ T shfl_down(T v, int d) { return __shfl_down_sync(SPMV_FULL_MASK, v, d); }
+template <typename T>
+__device__ __forceinline__ T shfl_idx(T v, int src) { return __shfl_sync(SPMV_FULL_MASK, v, src); }
+
+// exclusive prefix sum of an int over the warp
+__device__ __forceinline__ int warp_exclusive_scan(int v) {
+    const int lane = lane_id();
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int y = __shfl_up_sync(SPMV_FULL_MASK, x, d);
+        if (lane >= d) x += y;
+    }
+    return x - v;
+}
+
+// longest run of zero bits in a 32-bit mask (warp-uniform integer work)
+__device__ __forceinline__ int longest_zero_run(uint32_t mask) {
+    uint32_t y = ~mask;
+    int r = 0;
+    while (y) {
+        y &= y << 1;
+        ++r;
+    }
+    return r;
+}
+
+}  // namespace spmv

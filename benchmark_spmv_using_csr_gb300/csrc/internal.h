@@ -1,0 +1,66 @@
+// internal.h -- launchers shared between the library's translation units (not installed).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace spmv {
+
+inline int num_tiles(int nnz, int tile) { return (int)(((long long)nnz + tile - 1) / tile); }
+
+// Schedule of the plain / mixed tile kernels: S non-zeros per lane (tile = 32*S), a worker
+// (one warp) walks `tiles_per_worker` consecutive tiles, `warps_per_cta` workers per CTA.
+struct TileConfig {
+    int seg;               // S in {8, 16, 32}
+    int tiles_per_worker;  // >= 1
+    int warps_per_cta;     // 4 or 8
+};
+
+// partition.cu
+cudaError_t launch_partition(const int* row_ptr, int m, int nnz, int tile, uint32_t* tile_ptr,
+                             cudaStream_t st);
+cudaError_t launch_bitflags(const int* row_ptr, int m, int nnz, int seg, const uint32_t* tile_ptr,
+                            uint32_t* words, cudaStream_t st);
+cudaError_t launch_validate(const int* row_ptr, const int* col, int m, int n, int nnz,
+                            uint32_t* bad, cudaStream_t st);
+
+// spmv_plain.cu: plain forms (value type = accumulate type = FP64 or FP32)
+struct PlainLaunch {
+    const int* row_ptr;
+    const int* col;
+    const void* val;
+    const void* x;
+    void* y;
+    const uint32_t* tile_ptr;
+    int* rec_row;     // [nworkers]
+    void* rec_val;    // [nworkers] of the value type
+    uint32_t* err;
+    int m, n, nnz;
+    int phase;  // bit 0: tile kernel, bit 1: calibration kernel
+};
+cudaError_t launch_plain_f64(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
+cudaError_t launch_plain_f32(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
+
+// spmv_mixed.cu: mixed forms (FP32 / BF16 values, FP32 x and y, compensated FP32
+// accumulation, FP64 carries and records)
+struct MixedLaunch {
+    const int* row_ptr;
+    const int* col;
+    const void* val;  // float or __nv_bfloat16
+    const float* x;
+    float* y;
+    const uint32_t* tile_ptr;
+    int* rec_row;
+    double* rec_val;
+    uint32_t* err;
+    int m, n, nnz;
+    bool bf16;
+    int phase;  // bit 0: tile kernel, bit 1: calibration kernel
+};
+cudaError_t launch_mixed(const MixedLaunch& a, const TileConfig& cfg, cudaStream_t st);
+cudaError_t launch_convert_from_f64(const double* src, void* dst, size_t n, bool to_bf16,
+                                    cudaStream_t st);
+cudaError_t launch_convert_to_f64(const float* src, double* dst, size_t n, cudaStream_t st);
+
+inline bool is_supported_value_type(int vt) { return vt >= 0 && vt <= 3; }
+
+}  // namespace spmv

@@ -1,0 +1,110 @@
+// partition.cu -- tile_ptr construction (binary-search partition + dirty bits), the
+// bit-flag parity kernel, and the CSR validation pass run before a matrix is accepted.
+#include "internal.h"
+#include "tile.cuh"
+
+namespace spmv {
+
+// One thread per tile boundary: tile_ptr[t] = search_right(min(t*TILE, nnz)) - 1
+// (spmv_cuda/kernels_cuda.h:43-49).  The reference searches each boundary inside every
+// SpMV launch (twice for boundaries shared by adjacent warps); here it is done once per
+// matrix and reused by every call.
+__global__ void k_tile_rows(const int* __restrict__ row_ptr, int m, int nnz, int tile,
+                            int ntiles, uint32_t* __restrict__ tile_ptr) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > ntiles) return;
+    long long b = (long long)t * tile;
+    if (b > nnz) b = nnz;
+    tile_ptr[t] = (uint32_t)(search_right(row_ptr, (int)b, m + 1) - 1);
+}
+
+// One thread per row: an empty row r with o = row_ptr[r] lies strictly inside the span of
+// tile (o % TILE == 0 ? o/TILE - 1 : o/TILE) (clamped to the last tile), which is exactly
+// the tile whose span the reference scans and finds it in (kernels_cuda.h:119-145).
+// Leading empty rows (o == 0) belong to no tile.  Setting a bit is idempotent, so the
+// result does not depend on the order of the atomics.
+__global__ void k_mark_dirty(const int* __restrict__ row_ptr, int m, int tile, int ntiles,
+                             uint32_t* __restrict__ tile_ptr) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const int o = __ldg(row_ptr + r);
+        if (o != __ldg(row_ptr + r + 1)) continue;
+        int t = (o % tile == 0) ? o / tile - 1 : o / tile;
+        if (t > ntiles - 1) t = ntiles - 1;
+        if (t >= 0) atomicOr(tile_ptr + t, DIRTY_BIT);
+    }
+}
+
+// One warp per tile: the raw bit-flag words of every tile, produced by the same
+// tile_flags() the SpMV kernels use (exposed for parity against the reference's words).
+template <int S>
+__global__ void k_bitflags(const int* __restrict__ row_ptr, int m, int nnz, int ntiles,
+                           const uint32_t* __restrict__ tile_ptr, uint32_t* __restrict__ words) {
+    __shared__ uint32_t s_words[8][32];
+    const int warp = threadIdx.x >> 5;
+    const int t = blockIdx.x * 8 + warp;
+    if (t >= ntiles) return;
+    const uint32_t tp0 = tile_ptr[t], tp1 = tile_ptr[t + 1];
+    const uint32_t w = tile_flags<S, double>(row_ptr, m, t * 32 * S, (int)(tp0 & ROW_MASK),
+                                             (int)(tp1 & ROW_MASK), false, s_words[warp],
+                                             nullptr, 0, nullptr, nullptr);
+    words[(size_t)t * 32 + lane_id()] = w;
+    (void)nnz;
+}
+
+// CSR validation: row_ptr[0] == 0, non-decreasing, row_ptr[m] == nnz, 0 <= col < n.
+// Any violation sets a bit in *bad (bit0 row_ptr, bit1 col_idx).
+__global__ void k_validate(const int* __restrict__ row_ptr, const int* __restrict__ col, int m,
+                           int n, int nnz, uint32_t* bad) {
+    const int stride = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0 && (row_ptr[0] != 0 || row_ptr[m] != nnz)) atomicOr(bad, 1u);
+    for (int r = tid; r < m; r += stride)
+        if (__ldg(row_ptr + r) > __ldg(row_ptr + r + 1)) atomicOr(bad, 1u);
+    for (int e = tid; e < nnz; e += stride) {
+        const int c = __ldg(col + e);
+        if (c < 0 || c >= n) atomicOr(bad, 2u);
+    }
+}
+
+static int grid_for(long long work, int threads, int cap) {
+    long long g = (work + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}
+
+cudaError_t launch_partition(const int* row_ptr, int m, int nnz, int tile, uint32_t* tile_ptr,
+                             cudaStream_t st) {
+    const int nt = num_tiles(nnz, tile);
+    k_tile_rows<<<grid_for(nt + 1, 256, 1 << 20), 256, 0, st>>>(row_ptr, m, nnz, tile, nt,
+                                                                tile_ptr);
+    if (m > 0 && nt > 0)
+        k_mark_dirty<<<grid_for(m, 256, 152 * 16), 256, 0, st>>>(row_ptr, m, tile, nt, tile_ptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bitflags(const int* row_ptr, int m, int nnz, int seg, const uint32_t* tile_ptr,
+                            uint32_t* words, cudaStream_t st) {
+    const int nt = num_tiles(nnz, 32 * seg);
+    if (nt == 0) return cudaSuccess;
+    const int blocks = (nt + 7) / 8;
+    switch (seg) {
+        case 1: k_bitflags<1><<<blocks, 256, 0, st>>>(row_ptr, m, nnz, nt, tile_ptr, words); break;
+        case 2: k_bitflags<2><<<blocks, 256, 0, st>>>(row_ptr, m, nnz, nt, tile_ptr, words); break;
+        case 4: k_bitflags<4><<<blocks, 256, 0, st>>>(row_ptr, m, nnz, nt, tile_ptr, words); break;
+        case 8: k_bitflags<8><<<blocks, 256, 0, st>>>(row_ptr, m, nnz, nt, tile_ptr, words); break;
+        case 16: k_bitflags<16><<<blocks, 256, 0, st>>>(row_ptr, m, nnz, nt, tile_ptr, words); break;
+        case 32: k_bitflags<32><<<blocks, 256, 0, st>>>(row_ptr, m, nnz, nt, tile_ptr, words); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_validate(const int* row_ptr, const int* col, int m, int n, int nnz,
+                            uint32_t* bad, cudaStream_t st) {
+    long long work = (long long)(m > nnz ? m : nnz);
+    k_validate<<<grid_for(work, 256, 152 * 8), 256, 0, st>>>(row_ptr, col, m, n, nnz, bad);
+    return cudaGetLastError();
+}
+
+}  // namespace spmv

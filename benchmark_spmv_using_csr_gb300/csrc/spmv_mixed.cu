@@ -1,0 +1,115 @@
+// spmv_mixed.cu -- mixed-precision forms: values stored in FP32 or BF16, x and y in FP32,
+// products and the in-tile segmented sum in compensated FP32 (TwoProduct by FMA + TwoSum,
+// a float-float accumulator), carries between tiles and the calibration of rows that span
+// several tiles or workers in FP64.  No counterpart in the reference, which only has the
+// USE_DOUBLE switch (spmv_cuda/common.h:27-31).
+#include "internal.h"
+#include "tile_kernel.cuh"
+
+namespace spmv {
+
+// Error-free transforms with explicitly rounded intrinsics, so that nvcc cannot contract
+// or reassociate them (Knuth TwoSum; TwoProduct through the exact FMA residual).
+__device__ __forceinline__ float2 ff_add_product(float v, float x, float2 a) {
+    const float p = __fmul_rn(v, x);
+    const float ep = __fmaf_rn(v, x, -p);
+    const float s = __fadd_rn(a.x, p);
+    const float bb = __fsub_rn(s, a.x);
+    const float es = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    return make_float2(s, __fadd_rn(a.y, __fadd_rn(es, ep)));
+}
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    const float s = __fadd_rn(a.x, b.x);
+    const float bb = __fsub_rn(s, a.x);
+    const float es = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+    return make_float2(s, __fadd_rn(__fadd_rn(a.y, b.y), es));
+}
+
+template <typename VSTORE>
+struct PolMixed {
+    using VS = VSTORE;
+    using VC = float;
+    using XT = float;
+    using YT = float;
+    using Acc = float2;
+    using Carry = double;
+    __device__ static float2 zero() { return make_float2(0.f, 0.f); }
+    __device__ static double carry_zero() { return 0.0; }
+    __device__ static float2 fma(float v, float x, float2 a) { return ff_add_product(v, x, a); }
+    __device__ static float2 add(float2 a, float2 b) { return ff_add(a, b); }
+    __device__ static double carry_from(float2 a) { return (double)a.x + (double)a.y; }
+    __device__ static double carry_add(double c, float2 a) { return c + ((double)a.x + (double)a.y); }
+    __device__ static float out_acc(float2 a) { return __fadd_rn(a.x, a.y); }
+    __device__ static float out_carry(double c) { return __double2float_rn(c); }
+    __device__ static double carry_of_y(float y) { return (double)y; }
+};
+
+cudaError_t launch_mixed(const MixedLaunch& l, const TileConfig& cfg, cudaStream_t st) {
+    if (l.bf16) {
+        TileArgs<PolMixed<__nv_bfloat16>> a;
+        a.row_ptr = l.row_ptr;
+        a.col = l.col;
+        a.val = static_cast<const __nv_bfloat16*>(l.val);
+        a.x = l.x;
+        a.y = l.y;
+        a.tile_ptr = l.tile_ptr;
+        a.rec_row = l.rec_row;
+        a.rec_val = l.rec_val;
+        a.err = l.err;
+        a.m = l.m;
+        a.n = l.n;
+        a.nnz = l.nnz;
+        a.phase = l.phase;
+        return launch_tiles(a, cfg, st);
+    }
+    TileArgs<PolMixed<float>> a;
+    a.row_ptr = l.row_ptr;
+    a.col = l.col;
+    a.val = static_cast<const float*>(l.val);
+    a.x = l.x;
+    a.y = l.y;
+    a.tile_ptr = l.tile_ptr;
+    a.rec_row = l.rec_row;
+    a.rec_val = l.rec_val;
+    a.err = l.err;
+    a.m = l.m;
+    a.n = l.n;
+    a.nnz = l.nnz;
+    a.phase = l.phase;
+    return launch_tiles(a, cfg, st);
+}
+
+// FP64 -> FP32 or BF16 (round to nearest even), and FP32 -> FP64.
+__global__ void k_from_f64(const double* __restrict__ src, void* __restrict__ dst, size_t n,
+                           bool to_bf16) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (to_bf16)
+            static_cast<__nv_bfloat16*>(dst)[i] = __double2bfloat16(src[i]);
+        else
+            static_cast<float*>(dst)[i] = __double2float_rn(src[i]);
+    }
+}
+__global__ void k_to_f64(const float* __restrict__ src, double* __restrict__ dst, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += stride)
+        dst[i] = (double)src[i];
+}
+
+cudaError_t launch_convert_from_f64(const double* src, void* dst, size_t n, bool to_bf16,
+                                    cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    size_t g = (n + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_from_f64<<<(unsigned)g, 256, 0, st>>>(src, dst, n, to_bf16);
+    return cudaGetLastError();
+}
+cudaError_t launch_convert_to_f64(const float* src, double* dst, size_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    size_t g = (n + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_to_f64<<<(unsigned)g, 256, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+}  // namespace spmv

@@ -1,0 +1,153 @@
+/*
+ * spmv_gb300.h -- C ABI of the GB300 speculative segmented-sum CSR SpMV (y = A.x).
+ *
+ * Plain C: opaque handles, plain pointers and sizes.  Every function returns an int
+ * status (0 = success) and never aborts the process; the text of the last failure of a
+ * handle is available from bhsp_last_error().
+ *
+ * The handle API mirrors, call for call, the host class bhsparse_spmv_cuda of the
+ * reference (spmv_cuda/bhsparse_spmv_cuda.h:7-55); include/bhsparse_spmv_cuda.h wraps
+ * it back into that class.  The plan API below it runs the same kernels on buffers that
+ * the caller already holds in device memory.
+ */
+#ifndef SPMV_GB300_H
+#define SPMV_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The first two keep the reference's values (spmv_cuda/common.h:24-25). */
+#define BHSPARSE_SUCCESS 0
+#define BHSPARSE_UNSUPPORTED_VALUE_TYPE -1
+#define BHSPARSE_INVALID_ARGUMENT -2     /* bad size, null pointer, unknown config */
+#define BHSPARSE_INVALID_CSR -3          /* row_ptr not monotone / not ending at nnz, col out of range */
+#define BHSPARSE_CUDA_ERROR -4           /* a CUDA runtime call failed (see bhsp_last_error) */
+#define BHSPARSE_NOT_PREPARED -5         /* run/get before prepare_mem */
+#define BHSPARSE_DEVICE_CHECK_FAILED -6  /* a kernel's own bounds check fired */
+#define BHSPARSE_OUT_OF_MEMORY -7
+
+/* Largest nnz accepted (int32 indices with one tile of head-room). */
+#define BHSP_MAX_NNZ 2147479551
+
+/* Value types.  F64 / F32 are the reference's USE_DOUBLE=1 / USE_DOUBLE=0 builds
+ * (spmv_cuda/common.h:27-31).  The mixed forms take and return FP64 on the host side,
+ * store the matrix values in FP32 or BF16 and x / y in FP32, accumulate with a
+ * compensated (TwoSum) FP32 segmented sum and carry between tiles in FP64. */
+typedef enum {
+    BHSP_VALUE_F64 = 0,
+    BHSP_VALUE_F32 = 1,
+    BHSP_VALUE_MIXED_F32 = 2,
+    BHSP_VALUE_MIXED_BF16 = 3
+} bhsp_value_type;
+
+/* ------------------------------------------------------------------------------------ */
+/* Handle API: one object of the reference class bhsparse_spmv_cuda.                     */
+/* ------------------------------------------------------------------------------------ */
+typedef struct bhsp_spmv bhsp_spmv;
+
+/* Constructor, spmv_cuda/bhsparse_spmv_cuda.h:10, 57-59 (value type = the USE_DOUBLE choice). */
+int bhsp_create(bhsp_spmv** out, int value_type);
+/* Destructor (the reference object is deleted by the caller; frees whatever is left). */
+void bhsp_destroy(bhsp_spmv* h);
+/* init_platform, spmv_cuda/bhsparse_spmv_cuda.h:61-75: selects the device (0 unless
+ * bhsp_set_device chose another) and records its name. */
+int bhsp_init_platform(bhsp_spmv* h);
+/* free_platform, spmv_cuda/bhsparse_spmv_cuda.h:77-82. */
+int bhsp_free_platform(bhsp_spmv* h);
+/* prepare_mem, spmv_cuda/bhsparse_spmv_cuda.h:238-351: copies A (row_ptr, col_idx, val),
+ * x and the initial y into device memory, validates the CSR, builds the tile partition
+ * and keeps the caller's y pointer for get_y (the caller's y must outlive the object, as
+ * in the reference).  val / x / y are double* for F64 and the mixed forms, float* for F32. */
+int bhsp_prepare_mem(bhsp_spmv* h, int m, int n, int nnz, const int* row_ptr,
+                     const int* col_idx, const void* val, const void* x, void* y);
+/* run_benchmark, spmv_cuda/bhsparse_spmv_cuda.h:121-228: y = A.x on the device, including
+ * the calibration of rows that cross tiles and of empty rows; returns when done.  Unlike
+ * the reference, the result does not depend on y's previous contents and repeated calls
+ * give the same y. */
+int bhsp_run_benchmark(bhsp_spmv* h);
+/* get_y, spmv_cuda/bhsparse_spmv_cuda.h:230-236: copies y into the pointer given to
+ * prepare_mem.  Returns a status (the CUDA twin returns void; the OpenCL twin returns int,
+ * spmv_opencl_amd/bhsparse_spmv_opencl.h:401). */
+int bhsp_get_y(bhsp_spmv* h);
+/* free_mem, spmv_cuda/bhsparse_spmv_cuda.h:84-118. */
+int bhsp_free_mem(bhsp_spmv* h);
+/* Text of the last failure on this handle ("" if none). */
+const char* bhsp_last_error(const bhsp_spmv* h);
+
+/* -- additions with no counterpart in the reference -- */
+/* Choose the CUDA device used by init_platform (default 0, as the reference hard-codes). */
+int bhsp_set_device(bhsp_spmv* h, int device);
+/* Tile schedule: seg = non-zeros per lane (8, 16 or 32), tiles_per_worker >= 1,
+ * warps_per_cta 4 or 8.  Before prepare_mem; 0 for any field keeps the default. */
+int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int warps_per_cta);
+int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tiles_per_worker, int* warps_per_cta);
+/* Replace x (host pointer, same type as in prepare_mem) without rebuilding anything. */
+int bhsp_set_x(bhsp_spmv* h, const void* x);
+/* Enqueue y = A.x on `stream` (a cudaStream_t, NULL = the legacy default stream) and
+ * return at once; bhsp_check() synchronises and reports a kernel-side failure. */
+int bhsp_run_async(bhsp_spmv* h, void* stream);
+int bhsp_check(bhsp_spmv* h);
+/* One phase of bhsp_run_async: 1 = the tile kernel, 2 = the calibration kernel that adds
+ * the per-worker carry records, 3 = both.  Phase 2 must follow phase 1 on the same stream;
+ * exists so that the two kernels can be timed apart. */
+int bhsp_run_phase(bhsp_spmv* h, void* stream, int phase);
+/* Device pointers of the handle's buffers (for callers that keep working on the device). */
+int bhsp_device_buffers(const bhsp_spmv* h, const int** row_ptr, const int** col_idx,
+                        const void** val, void** x, void** y);
+/* Bytes of device memory the handle holds. */
+size_t bhsp_device_bytes(const bhsp_spmv* h);
+
+/* ------------------------------------------------------------------------------------ */
+/* Plan API: the same kernels over device buffers the caller owns.                       */
+/* ------------------------------------------------------------------------------------ */
+typedef struct bhsp_plan bhsp_plan;
+
+/* Validates the CSR on the device, builds tile_ptr and allocates the carry records.
+ * row_ptr / col_idx stay owned by the caller and must outlive the plan.
+ * seg / tiles_per_worker / warps_per_cta as in bhsp_set_config (0 = default). */
+int bhsp_plan_create(bhsp_plan** out, int value_type, int m, int n, int nnz,
+                     const int* d_row_ptr, const int* d_col_idx, int seg, int tiles_per_worker,
+                     int warps_per_cta, void* stream);
+/* y = A.x, enqueued on `stream`.  d_val in the storage type of value_type (double, float,
+ * float, __nv_bfloat16), d_x / d_y in the x/y type (double for F64, float otherwise). */
+int bhsp_plan_execute(bhsp_plan* p, const void* d_val, const void* d_x, void* d_y, void* stream);
+/* One phase of bhsp_plan_execute (1 = tile kernel, 2 = calibration, 3 = both). */
+int bhsp_plan_execute_phase(bhsp_plan* p, const void* d_val, const void* d_x, void* d_y,
+                            void* stream, int phase);
+/* Synchronise `stream` and report (then clear) any kernel-side check that fired. */
+int bhsp_plan_check(bhsp_plan* p, void* stream);
+/* Number of device kernels one bhsp_plan_execute launches. */
+int bhsp_plan_launches(const bhsp_plan* p);
+/* tile_ptr of the plan (device pointer, ntiles+1 entries) and its tile size. */
+int bhsp_plan_tiles(const bhsp_plan* p, const uint32_t** d_tile_ptr, int* ntiles, int* tile_nnz);
+const char* bhsp_plan_last_error(const bhsp_plan* p);
+void bhsp_plan_destroy(bhsp_plan* p);
+
+/* ------------------------------------------------------------------------------------ */
+/* Partition primitives (device pointers), exposed for parity checks.                    */
+/* ------------------------------------------------------------------------------------ */
+/* tile_ptr[t], t = 0..ceil(nnz/tile_nnz): the row of boundary min(t*tile_nnz, nnz) found by
+ * the right-boundary binary search (spmv_cuda/utils_cuda.h:6-31, kernels_cuda.h:39-53),
+ * bit 31 set when tile t holds an empty row (kernels_cuda.h:119-145). */
+int bhsp_partition(const int* d_row_ptr, int m, int nnz, int tile_nnz, uint32_t* d_tile_ptr,
+                   void* stream);
+/* Raw bit-flag words, 32 per tile of 32*seg non-zeros (kernels_cuda.h:114-148, before the
+ * lane-0 head bit is forced at :172).  seg in {1,2,4,8,16,32}; d_words may be NULL when
+ * nnz == 0 (there are no tiles). */
+int bhsp_bitflags(const int* d_row_ptr, int m, int nnz, int seg, const uint32_t* d_tile_ptr,
+                  uint32_t* d_words, void* stream);
+/* 0 if the CSR is valid, else BHSPARSE_INVALID_CSR (synchronises `stream`). */
+int bhsp_validate_csr(const int* d_row_ptr, const int* d_col_idx, int m, int n, int nnz,
+                      void* stream);
+
+/* Library version string and the compute capability it was built for. */
+const char* bhsp_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPMV_GB300_H */

@@ -1,0 +1,257 @@
+"""ctypes bindings of ``oracle.c`` (the C restatement of the reference path).
+
+Test infrastructure only.  Each wrapper names the reference code it restates
+(paths relative to the reference project):
+
+* :func:`partition`         spmv_cuda/utils_cuda.h:6-31, spmv_cuda/kernels_cuda.h:39-53, 114-145
+* :func:`bitflags`          spmv_cuda/kernels_cuda.h:114-148
+* :func:`bhsparse`          spmv_cuda/kernels_cuda.h:7-269 + spmv_cuda/bhsparse_spmv_cuda.h:166-222
+* :func:`csr_serial`        spmv_cuda/main.cu:755-761
+* :func:`csr_omp`           spmv_cuda/main.cu:370-393
+* :func:`csr_dot2`          FP64 compensated oracle (Ogita-Rump-Oishi Dot2)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SO = os.path.join(_HERE, "_build", "liboracle.so")
+_lock = threading.Lock()
+_lib = None
+
+LANES = 32  # THREADBUNCH, spmv_cuda/common.h:39
+STEP = 7    # spmv_cuda/common.h:48
+SEG_H_F64 = 4  # spmv_cuda/common.h:43
+SEG_H_F32 = 8  # spmv_cuda/common.h:45
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_f32p = ctypes.POINTER(ctypes.c_float)
+
+
+def build() -> str:
+    """Compile ``oracle.c`` with its Makefile (idempotent)."""
+    src = os.path.join(_HERE, "oracle.c")
+    if not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _SO
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    with _lock:
+        if _lib is None:
+            _lib = ctypes.CDLL(build())
+            L = _lib
+            L.oracle_search_right.argtypes = [_i32p, ctypes.c_int, ctypes.c_int]
+            L.oracle_search_right.restype = ctypes.c_int
+            L.oracle_num_tiles.argtypes = [ctypes.c_int, ctypes.c_int]
+            L.oracle_num_tiles.restype = ctypes.c_int
+            L.oracle_num_warps.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+            L.oracle_num_warps.restype = ctypes.c_int
+            L.oracle_partition.argtypes = [_i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u32p]
+            L.oracle_partition.restype = None
+            L.oracle_bitflags.argtypes = [_i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, _u32p, _u32p]
+            L.oracle_bitflags.restype = None
+            for name, vp in (("oracle_bhsparse_f64", _f64p), ("oracle_bhsparse_f32", _f32p)):
+                f = getattr(L, name)
+                f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _i32p, vp, vp,
+                              ctypes.c_int, ctypes.c_int, vp, _i32p, vp, _i32p, _i32p, _i32p]
+                f.restype = ctypes.c_int
+            L.oracle_csr_serial_f64.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+            L.oracle_csr_serial_f32.argtypes = [ctypes.c_int, _i32p, _i32p, _f32p, _f32p, _f32p]
+            L.oracle_csr_serial_rows_f64.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p,
+                                                     _f64p, _f64p, _f64p]
+            L.oracle_csr_omp_f64.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _f64p, _f64p,
+                                             ctypes.c_int]
+            L.oracle_csr_omp_f32.argtypes = [ctypes.c_int, _i32p, _i32p, _f32p, _f32p, _f32p,
+                                             ctypes.c_int]
+            L.oracle_csr_dot2.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _f64p, _f64p,
+                                          ctypes.c_int]
+            L.oracle_csr_absrow.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _f64p, _f64p,
+                                            ctypes.c_int]
+            L.oracle_max_threads.restype = ctypes.c_int
+        return _lib
+
+
+def _p(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+def _c(a, dtype) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def num_tiles(nnz: int, ps: int) -> int:
+    return int(lib().oracle_num_tiles(int(nnz), int(ps)))
+
+
+def num_warps(nnz: int, seg_h: int, step: int = STEP) -> int:
+    return int(lib().oracle_num_warps(int(nnz), int(seg_h), int(step)))
+
+
+def search_right(row_ptr, key: int) -> int:
+    rp = _c(row_ptr, np.int32)
+    return int(lib().oracle_search_right(_p(rp, _i32p), int(key), rp.size))
+
+
+def partition(row_ptr, nnz: int, ps: int) -> np.ndarray:
+    """tile_ptr[0..ntiles] as uint32: row of boundary t*ps, bit 31 = tile t dirty."""
+    rp = _c(row_ptr, np.int32)
+    m = rp.size - 1
+    out = np.zeros(num_tiles(nnz, ps) + 1, dtype=np.uint32)
+    lib().oracle_partition(_p(rp, _i32p), m, int(nnz), int(ps), _p(out, _u32p))
+    return out
+
+
+def bitflags(row_ptr, nnz: int, lanes: int, seg: int, tile_ptr=None) -> np.ndarray:
+    """Raw bit-flag words, shape (ntiles, lanes), before lane 0's head bit is forced."""
+    rp = _c(row_ptr, np.int32)
+    m = rp.size - 1
+    ps = lanes * seg
+    if tile_ptr is None:
+        tile_ptr = partition(rp, nnz, ps)
+    tp = _c(tile_ptr, np.uint32)
+    nt = num_tiles(nnz, ps)
+    out = np.zeros((nt, lanes), dtype=np.uint32)
+    lib().oracle_bitflags(_p(rp, _i32p), m, int(nnz), int(lanes), int(seg), _p(tp, _u32p),
+                          _p(out, _u32p))
+    return out
+
+
+class BhsparseResult:
+    """Everything the simulated reference kernel + host calibration produce."""
+
+    def __init__(self, y, sync_idx, sync_val, spec, ndirty, oob_guarded):
+        self.y = y
+        self.sync_idx = sync_idx
+        self.sync_val = sync_val
+        self.speculator = spec
+        self.ndirty = ndirty
+        self.oob_guarded = oob_guarded
+
+
+def bhsparse(row_ptr, col, val, x, n: int | None = None, seg_h: int | None = None,
+             step: int = STEP, y0=None) -> BhsparseResult:
+    """Lane-level simulation of SpMV_kernel + run_benchmark's host calibration.
+
+    The value type follows ``val.dtype`` (float64 -> USE_DOUBLE=1, float32 ->
+    USE_DOUBLE=0).  ``y0`` is the y the object holds before the call (zeros,
+    as spmv_cuda/main.cu:769 sets it, when omitted).
+    """
+    rp = _c(row_ptr, np.int32)
+    ci = _c(col, np.int32)
+    m = rp.size - 1
+    nnz = int(rp[-1]) if m >= 0 else 0
+    if np.asarray(val).dtype == np.float32:
+        vt, vp, fn = np.float32, _f32p, lib().oracle_bhsparse_f32
+        seg_h = SEG_H_F32 if seg_h is None else seg_h
+    else:
+        vt, vp, fn = np.float64, _f64p, lib().oracle_bhsparse_f64
+        seg_h = SEG_H_F64 if seg_h is None else seg_h
+    v = _c(val, vt)
+    xx = _c(x, vt)
+    n = xx.size if n is None else n
+    y = np.zeros(max(m, 1), dtype=vt) if y0 is None else _c(y0, vt).copy()
+    nw = num_warps(nnz, seg_h, step)
+    sidx = np.zeros(max(nw, 1), dtype=np.int32)
+    sval = np.zeros(max(nw, 1), dtype=vt)
+    spec = np.zeros(2 * max(num_tiles(nnz, LANES * seg_h), 1), dtype=np.int32)
+    nd = ctypes.c_int(0)
+    fl = ctypes.c_int(0)
+    rc = fn(m, int(n), nnz, _p(rp, _i32p), _p(ci, _i32p), _p(v, vp), _p(xx, vp), int(seg_h),
+            int(step), _p(y, vp), _p(sidx, _i32p), _p(sval, vp), _p(spec, _i32p),
+            ctypes.byref(nd), ctypes.byref(fl))
+    if rc < 0:
+        raise ValueError("unsupported geometry")
+    return BhsparseResult(y[:m], sidx[:nw], sval[:nw], spec[:2 * nd.value].reshape(-1, 2),
+                          nd.value, bool(fl.value & 1))
+
+
+def csr_serial(row_ptr, col, val, x) -> np.ndarray:
+    rp, ci = _c(row_ptr, np.int32), _c(col, np.int32)
+    m = rp.size - 1
+    if np.asarray(val).dtype == np.float32:
+        v, xx = _c(val, np.float32), _c(x, np.float32)
+        y = np.zeros(max(m, 1), np.float32)
+        lib().oracle_csr_serial_f32(m, _p(rp, _i32p), _p(ci, _i32p), _p(v, _f32p),
+                                    _p(xx, _f32p), _p(y, _f32p))
+    else:
+        v, xx = _c(val, np.float64), _c(x, np.float64)
+        y = np.zeros(max(m, 1), np.float64)
+        lib().oracle_csr_serial_f64(m, _p(rp, _i32p), _p(ci, _i32p), _p(v, _f64p),
+                                    _p(xx, _f64p), _p(y, _f64p))
+    return y[:m]
+
+
+def csr_serial_rows(row_ptr, col, val, x, y, r0: int, r1: int) -> None:
+    """Serial loop over rows [r0, r1) into ``y`` (float64 arrays, no copies)."""
+    lib().oracle_csr_serial_rows_f64(int(r0), int(r1), _p(row_ptr, _i32p), _p(col, _i32p),
+                                     _p(val, _f64p), _p(x, _f64p), _p(y, _f64p))
+
+
+def csr_omp(row_ptr, col, val, x, nthreads: int = 0, y=None) -> np.ndarray:
+    rp, ci = _c(row_ptr, np.int32), _c(col, np.int32)
+    m = rp.size - 1
+    if np.asarray(val).dtype == np.float32:
+        v, xx = _c(val, np.float32), _c(x, np.float32)
+        y = np.zeros(max(m, 1), np.float32) if y is None else y
+        lib().oracle_csr_omp_f32(m, _p(rp, _i32p), _p(ci, _i32p), _p(v, _f32p), _p(xx, _f32p),
+                                 _p(y, _f32p), int(nthreads))
+    else:
+        v, xx = _c(val, np.float64), _c(x, np.float64)
+        y = np.zeros(max(m, 1), np.float64) if y is None else y
+        lib().oracle_csr_omp_f64(m, _p(rp, _i32p), _p(ci, _i32p), _p(v, _f64p), _p(xx, _f64p),
+                                 _p(y, _f64p), int(nthreads))
+    return y[:m]
+
+
+def csr_dot2(row_ptr, col, val, x, nthreads: int = 0) -> np.ndarray:
+    """FP64 compensated y* (Dot2 per row); val/x are taken as float64."""
+    rp, ci = _c(row_ptr, np.int32), _c(col, np.int32)
+    v, xx = _c(val, np.float64), _c(x, np.float64)
+    m = rp.size - 1
+    y = np.zeros(max(m, 1), np.float64)
+    lib().oracle_csr_dot2(m, _p(rp, _i32p), _p(ci, _i32p), _p(v, _f64p), _p(xx, _f64p),
+                          _p(y, _f64p), int(nthreads))
+    return y[:m]
+
+
+def csr_absrow(row_ptr, col, val, x, nthreads: int = 0) -> np.ndarray:
+    """(|A|.|x|)_i in float64: the scale of the componentwise tolerance."""
+    rp, ci = _c(row_ptr, np.int32), _c(col, np.int32)
+    v, xx = _c(val, np.float64), _c(x, np.float64)
+    m = rp.size - 1
+    y = np.zeros(max(m, 1), np.float64)
+    lib().oracle_csr_absrow(m, _p(rp, _i32p), _p(ci, _i32p), _p(v, _f64p), _p(xx, _f64p),
+                            _p(y, _f64p), int(nthreads))
+    return y[:m]
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
+
+
+def componentwise_error(y, y_star, absrow) -> float:
+    """max_i |y_i - y*_i| / (|A|.|x|)_i over rows with a non-zero scale."""
+    y = np.asarray(y, np.float64)
+    d = np.abs(y - y_star)
+    s = np.asarray(absrow, np.float64)
+    nz = s > 0
+    if (~nz).any() and np.any(d[~nz] != 0):
+        return float("inf")
+    return float((d[nz] / s[nz]).max()) if nz.any() else 0.0
+
+
+def normwise_error(y, y_star) -> float:
+    """||y - y*||_2 / ||y*||_2."""
+    y = np.asarray(y, np.float64)
+    den = np.linalg.norm(y_star)
+    return float(np.linalg.norm(y - y_star) / den) if den > 0 else float(np.linalg.norm(y))

@@ -1,0 +1,222 @@
+"""GPU parity of y = A.x through the C ABI (handle API = the reference's class, plan API =
+device buffers) against the oracle.
+
+Tolerances (stated here, componentwise relative to (|A|.|x|)_i against the FP64 compensated
+oracle y*): FP64 <= 1e-12, FP32 <= 1e-5; integer-valued data bit-exact against the serial
+loop (the reference's own check, spmv_cuda/main.cu:789-806); mixed forms <= 1e-6 normwise.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import TOL_F32, TOL_F64, TOL_MIXED_NORMWISE
+
+import benchmark_spmv_using_csr_gb300 as sp
+from benchmark_spmv_using_csr_gb300 import gen
+
+pytestmark = pytest.mark.gpu
+
+CONFIGS = [(8, 1, 4), (8, 3, 8), (16, 1, 8), (16, 5, 4), (32, 1, 4), (32, 2, 8), (32, 4, 8),
+           (32, 9, 4)]
+
+
+def run_handle(vt, rp, col, val, x, cfg=None, y0=None, repeat=1):
+    m = rp.size - 1
+    n = x.size
+    dt = sp.host_dtype(vt)
+    s = sp.BhsparseSpmvCuda(vt)
+    if cfg is not None:
+        assert s.set_config(*cfg) == 0
+    assert s.init_platform() == 0, s.last_error
+    y = np.zeros(max(m, 1), dt) if y0 is None else np.ascontiguousarray(y0, dt)
+    rc = s.prepare_mem(m, n, int(rp[-1]), rp, col, val.astype(dt), x.astype(dt), y)
+    assert rc == 0, s.last_error
+    for _ in range(repeat):
+        assert s.run_benchmark() == 0, s.last_error
+    assert s.get_y() == 0, s.last_error
+    assert s.free_mem() == 0
+    s.close()
+    return y[:m].copy()
+
+
+def int_csr(rng, m=None, n=None, maxlen=None, empty=None):
+    m = int(rng.integers(1, 6000)) if m is None else m
+    maxlen = int(rng.choice([3, 12, 60, 400, 2500])) if maxlen is None else maxlen
+    lens = rng.integers(0, maxlen, m)
+    e = rng.choice([0.0, 0.05, 0.4]) if empty is None else empty
+    lens[rng.random(m) < e] = 0
+    rp = np.zeros(m + 1, np.int32)
+    rp[1:] = np.cumsum(lens)
+    n = int(rng.integers(1, 7000)) if n is None else n
+    col = np.concatenate([np.sort(rng.choice(n, min(int(l), n), replace=False)) for l in lens]
+                         ).astype(np.int32) if rp[-1] else np.zeros(0, np.int32)
+    rp[1:] = np.cumsum(np.minimum(lens, n))
+    val = rng.integers(-9, 10, int(rp[-1])).astype(np.float64)
+    x = rng.integers(-9, 10, n).astype(np.float64)
+    return rp, col, val, x
+
+
+def test_known_6x6_all_forms(cuda_ok):
+    rp = np.array([0, 3, 9, 11, 11, 12, 15], np.int32)
+    col = np.array([0, 2, 5, 0, 1, 2, 3, 4, 5, 2, 4, 4, 2, 3, 4], np.int32)
+    val = np.arange(1, 16, dtype=np.float64)
+    x = np.ones(6)
+    for vt in (sp.VALUE_F64, sp.VALUE_F32, sp.VALUE_MIXED_F32, sp.VALUE_MIXED_BF16):
+        for cfg in CONFIGS[:3]:
+            y = run_handle(vt, rp, col, val, x, cfg)
+            assert y.astype(np.float64).tolist() == [6, 39, 21, 0, 12, 42], (vt, cfg)
+
+
+@pytest.mark.parametrize("vt", [sp.VALUE_F64, sp.VALUE_F32])
+def test_golden_cases_bit_exact(cuda_ok, golden_cases, vt):
+    d, names = golden_cases
+    for name in names:
+        rp, col, val, x = (d[f"{name}.{k}"] for k in ("row_ptr", "col", "val", "x"))
+        for cfg in CONFIGS:
+            y = run_handle(vt, rp, col, val, x, cfg)
+            assert np.array_equal(y.astype(np.float64), d[f"{name}.y"]), (name, cfg)
+
+
+@pytest.mark.parametrize("vt", [sp.VALUE_F64, sp.VALUE_F32])
+def test_random_integer_matrices_bit_exact(cuda_ok, vt):
+    rng = np.random.default_rng(99 + vt)
+    for i in range(40):
+        rp, col, val, x = int_csr(rng)
+        yr = oracle.csr_serial(rp, col, val, x)
+        cfg = CONFIGS[i % len(CONFIGS)]
+        y = run_handle(vt, rp, col, val, x, cfg)
+        assert np.array_equal(y.astype(np.float64), yr), (i, cfg)
+
+
+def test_y_contents_and_repeated_calls(cuda_ok):
+    """Unlike the reference (which needs y zeroed, bhsparse_spmv_cuda.h:170-173), the result
+    is independent of y's previous contents and stable across calls."""
+    rng = np.random.default_rng(5)
+    rp, col, val, x = int_csr(rng, m=5000, maxlen=80, empty=0.1)
+    yr = oracle.csr_serial(rp, col, val, x)
+    y = run_handle(sp.VALUE_F64, rp, col, val, x, (8, 1, 4), y0=np.full(5000, 7.5), repeat=5)
+    assert np.array_equal(y, yr)
+
+
+def _real_case(rng, kind):
+    if kind == "powerlaw":
+        a = gen.powerlaw(30000, seed=int(rng.integers(1 << 30)))
+    elif kind == "stencil27":
+        a = gen.stencil3d(24, 20, 17, seed=int(rng.integers(1 << 30)))
+    elif kind == "stencil5":
+        a = gen.stencil2d(97, 131, seed=int(rng.integers(1 << 30)))
+    elif kind == "dense_row":
+        a = gen.mixed_rows(20000, 30000, dense_row=777, mean_len=5, empty_frac=0.2,
+                           seed=int(rng.integers(1 << 30)))
+    elif kind == "empty90":
+        a = gen.mixed_rows(50000, 20000, mean_len=12, empty_frac=0.9, seed=int(rng.integers(1 << 30)))
+    else:
+        a = gen.blockdiag(9000, 9000, 32)
+    x = gen.uniform(a.n, int(rng.integers(1 << 30)))
+    return a, x
+
+
+KINDS = ["powerlaw", "stencil27", "stencil5", "dense_row", "empty90", "blockdiag"]
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_real_valued_fp64_tolerance(cuda_ok, kind):
+    rng = np.random.default_rng(KINDS.index(kind))
+    a, x = _real_case(rng, kind)
+    ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)
+    scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, x)
+    for cfg in CONFIGS[::2]:
+        y = run_handle(sp.VALUE_F64, a.row_ptr, a.col, a.val, x, cfg)
+        assert oracle.componentwise_error(y, ystar, scale) <= TOL_F64, cfg
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_real_valued_fp32_tolerance(cuda_ok, kind):
+    rng = np.random.default_rng(100 + KINDS.index(kind))
+    a, x = _real_case(rng, kind)
+    v32, x32 = a.val.astype(np.float32), x.astype(np.float32)
+    ystar = oracle.csr_dot2(a.row_ptr, a.col, v32.astype(np.float64), x32.astype(np.float64))
+    scale = oracle.csr_absrow(a.row_ptr, a.col, v32.astype(np.float64), x32.astype(np.float64))
+    for cfg in CONFIGS[1::2]:
+        y = run_handle(sp.VALUE_F32, a.row_ptr, a.col, v32, x32, cfg)
+        assert oracle.componentwise_error(y, ystar, scale) <= TOL_F32, cfg
+
+
+def bf16_round(v):
+    m, e = np.frexp(np.asarray(v, np.float64))
+    return np.ldexp(np.round(m * 256.0), e - 8)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_mixed_forms_normwise(cuda_ok, kind):
+    rng = np.random.default_rng(200 + KINDS.index(kind))
+    a, x = _real_case(rng, kind)
+    ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)
+    y = run_handle(sp.VALUE_MIXED_F32, a.row_ptr, a.col, a.val, x, (32, 4, 8))
+    assert oracle.normwise_error(y, ystar) <= TOL_MIXED_NORMWISE
+    # BF16 storage: the arithmetic is judged against y* of the BF16-rounded values and FP32 x
+    yb = run_handle(sp.VALUE_MIXED_BF16, a.row_ptr, a.col, a.val, x, (32, 4, 8))
+    ystar_b = oracle.csr_dot2(a.row_ptr, a.col, bf16_round(a.val),
+                              x.astype(np.float32).astype(np.float64))
+    assert oracle.normwise_error(yb, ystar_b) <= TOL_MIXED_NORMWISE
+
+
+def test_edge_shapes(cuda_ok):
+    cases = []
+    cases.append((np.zeros(5, np.int32), np.zeros(0, np.int32), np.zeros(0), np.ones(3)))  # m=4, nnz=0
+    cases.append((np.array([0, 1], np.int32), np.array([0], np.int32), np.array([3.0]), np.array([2.0])))
+    rp = np.array([0, 0, 0, 2000, 2000], np.int32)
+    cases.append((rp, np.arange(2000, dtype=np.int32), np.ones(2000), np.ones(2000)))
+    for rp, col, val, x in cases:
+        yr = oracle.csr_serial(rp, col, val, x)
+        for vt in (sp.VALUE_F64, sp.VALUE_F32):
+            for cfg in CONFIGS:
+                y = run_handle(vt, rp, col, val, x, cfg, y0=np.full(rp.size - 1, 3.0))
+                assert np.array_equal(y.astype(np.float64), yr), (rp.size, vt, cfg)
+
+
+def test_invalid_csr_is_rejected(cuda_ok):
+    s = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    y = np.zeros(2)
+    rc = s.prepare_mem(2, 2, 2, np.array([0, 1, 2], np.int32), np.array([0, 5], np.int32),
+                       np.ones(2), np.ones(2), y)
+    assert rc == sp.BHSPARSE_INVALID_CSR
+    rc = s.prepare_mem(2, 2, 2, np.array([0, 2, 1], np.int32), np.array([0, 1], np.int32),
+                       np.ones(2), np.ones(2), y)
+    assert rc == sp.BHSPARSE_INVALID_CSR
+    assert s.run_benchmark() == sp.BHSPARSE_NOT_PREPARED
+    s.close()
+
+
+def test_plan_api_on_torch_tensors(cuda_ok):
+    import torch
+    rng = np.random.default_rng(17)
+    a = gen.powerlaw(50000, seed=5)
+    x = gen.uniform(a.n, 6)
+    rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
+    val, xd = torch.from_numpy(a.val).cuda(), torch.from_numpy(x).cuda()
+    y = torch.full((a.m,), float("nan"), dtype=torch.float64, device="cuda")
+    p = sp.Plan(sp.VALUE_F64, a.m, a.n, rp, ci)
+    assert p.launches == 2
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        p.execute(val, xd, y)
+        p.check()
+    ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)
+    scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, x)
+    assert oracle.componentwise_error(y.cpu().numpy(), ystar, scale) <= TOL_F64
+    del rng
+
+
+def test_set_x_reuses_the_matrix(cuda_ok):
+    a = gen.stencil2d(64, 64)
+    x1, x2 = gen.uniform(a.n, 1), gen.uniform(a.n, 2)
+    s = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    y = np.zeros(a.m)
+    assert s.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x1, y) == 0
+    for xx in (x2, x1, x2):
+        assert s.set_x(xx) == 0
+        assert s.run_benchmark() == 0 and s.get_y() == 0
+        scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, xx)
+        assert oracle.componentwise_error(y, oracle.csr_dot2(a.row_ptr, a.col, a.val, xx), scale) <= TOL_F64
+    s.close()
