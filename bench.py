@@ -220,7 +220,6 @@ def run_ours(args) -> None:
 
     a, x = make_workload(args.workload)
     B = alg_bytes(a.m, a.n, a.nnz, 8, 8, 8)
-    seg, tpw, warps = args.config
 
     def barrier():
         if dist is not None:
@@ -231,7 +230,9 @@ def run_ours(args) -> None:
     y_pin = torch.zeros(a.m, dtype=torch.float64).pin_memory()
     y_np = y_pin.numpy()
     h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
-    assert h.set_config(seg, tpw, warps) == 0, h.last_error
+    if args.config is not None:
+        assert h.set_config(*args.config) == 0, h.last_error
+    seg, tpw, warps, stages = h.get_config()
     assert h.set_device(local) == 0
     assert h.init_platform() == 0, h.last_error
     t_prep = time.perf_counter()
@@ -329,7 +330,7 @@ def run_ours(args) -> None:
                        "m": a.m, "n": a.n, "nnz": a.nnz, "bytes_per_step": B,
                        "reference_formula_bytes": reference_formula_bytes(a.m, a.nnz, 8),
                        "tile": {"nnz_per_lane": seg, "tiles_per_worker": tpw,
-                                "warps_per_cta": warps},
+                                "warps_per_cta": warps, "tma_stages": stages},
                        "l2": "256 MiB flush write before every timed step; A (0.7 GB) > L2",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "pct_peak": round(100.0 * value / peak, 2),
@@ -429,8 +430,9 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--workload", choices=tuple(WORKLOAD_TEXT), default="powerlaw_4m")
-    ap.add_argument("--config", type=int, nargs=3, default=(32, 4, 8),
-                    metavar=("NNZ_PER_LANE", "TILES_PER_WORKER", "WARPS_PER_CTA"))
+    ap.add_argument("--config", type=int, nargs=4, default=None,
+                    metavar=("NNZ_PER_LANE", "TILES_PER_WORKER", "WARPS_PER_CTA", "STAGES"),
+                    help="tile schedule (default: the library's default)")
     ap.add_argument("--soak", type=float, default=1.5, help="seconds of untimed steps for clocks")
     ap.add_argument("--cpu-baseline", type=float, default=10.0,
                     help="seconds of serial CPU baseline (0 = skip)")

@@ -35,8 +35,8 @@ SIGNATURES = {
     "bhsp_free_mem": (c_int, [c_void_p]),
     "bhsp_last_error": (c_char_p, [c_void_p]),
     "bhsp_set_device": (c_int, [c_void_p, c_int]),
-    "bhsp_set_config": (c_int, [c_void_p, c_int, c_int, c_int]),
-    "bhsp_get_config": (c_int, [c_void_p, P_int, P_int, P_int]),
+    "bhsp_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
+    "bhsp_get_config": (c_int, [c_void_p, P_int, P_int, P_int, P_int]),
     "bhsp_set_x": (c_int, [c_void_p, c_void_p]),
     "bhsp_run_async": (c_int, [c_void_p, c_void_p]),
     "bhsp_check": (c_int, [c_void_p]),
@@ -45,7 +45,7 @@ SIGNATURES = {
     "bhsp_device_bytes": (c_size_t, [c_void_p]),
     # plan API
     "bhsp_plan_create": (c_int, [P_void, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int,
-                                 c_int, c_int, c_void_p]),
+                                 c_int, c_int, c_int, c_void_p]),
     "bhsp_plan_execute": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "bhsp_plan_execute_phase": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]),
     "bhsp_plan_check": (c_int, [c_void_p, c_void_p]),

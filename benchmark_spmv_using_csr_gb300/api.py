@@ -38,7 +38,8 @@ VALUE_MIXED_BF16 = 3
 VALUE_NAMES = {VALUE_F64: "f64", VALUE_F32: "f32", VALUE_MIXED_F32: "mixed_f32",
                VALUE_MIXED_BF16: "mixed_bf16"}
 
-DEFAULT_CONFIG = (32, 4, 8)  # (non-zeros per lane, tiles per worker, warps per CTA)
+# (non-zeros per lane, tiles per worker, warps per CTA, TMA stages; 0 stages = direct loads)
+DEFAULT_CONFIG = (16, 8, 4, 0)
 
 
 class SpmvError(RuntimeError):
@@ -113,13 +114,16 @@ class BhsparseSpmvCuda:
     def set_device(self, device: int) -> int:
         return self._L.bhsp_set_device(self._h, int(device))
 
-    def set_config(self, seg: int = 0, tiles_per_worker: int = 0, warps_per_cta: int = 0) -> int:
-        return self._L.bhsp_set_config(self._h, int(seg), int(tiles_per_worker), int(warps_per_cta))
+    def set_config(self, seg: int = 0, tiles_per_worker: int = 0, warps_per_cta: int = 0,
+                   stages: int = -1) -> int:
+        return self._L.bhsp_set_config(self._h, int(seg), int(tiles_per_worker), int(warps_per_cta),
+                                       int(stages))
 
-    def get_config(self) -> tuple[int, int, int]:
-        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        self._L.bhsp_get_config(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
-        return a.value, b.value, c.value
+    def get_config(self) -> tuple[int, int, int, int]:
+        a, b, c, d = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._L.bhsp_get_config(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                ctypes.byref(d))
+        return a.value, b.value, c.value, d.value
 
     def set_x(self, x) -> int:
         xx = np.ascontiguousarray(x, dtype=host_dtype(self.value_type))
@@ -178,7 +182,8 @@ class Plan:
     """
 
     def __init__(self, value_type: int, m: int, n: int, row_ptr, col_idx, nnz: int | None = None,
-                 seg: int = 0, tiles_per_worker: int = 0, warps_per_cta: int = 0, stream=None):
+                 seg: int = 0, tiles_per_worker: int = 0, warps_per_cta: int = 0, stages: int = -1,
+                 stream=None):
         self._L = lib()
         self.value_type = int(value_type)
         self.m, self.n = int(m), int(n)
@@ -187,7 +192,7 @@ class Plan:
         self._p = ctypes.c_void_p()
         rc = self._L.bhsp_plan_create(ctypes.byref(self._p), self.value_type, self.m, self.n,
                                       self.nnz, row_ptr.data_ptr(), col_idx.data_ptr(), int(seg),
-                                      int(tiles_per_worker), int(warps_per_cta),
+                                      int(tiles_per_worker), int(warps_per_cta), int(stages),
                                       ctypes.c_void_p(_stream_ptr(stream)))
         if rc != BHSPARSE_SUCCESS:
             raise SpmvError(rc, "bhsp_plan_create failed")

@@ -11,9 +11,10 @@ using namespace spmv;
 
 namespace {
 
-constexpr int kDefaultSeg = 32;
-constexpr int kDefaultTpw = 4;
-constexpr int kDefaultWarps = 8;
+constexpr int kDefaultSeg = 16;
+constexpr int kDefaultTpw = 8;
+constexpr int kDefaultWarps = 4;
+constexpr int kDefaultStages = 0;
 
 bool valid_vt(int vt) { return vt >= BHSP_VALUE_F64 && vt <= BHSP_VALUE_MIXED_BF16; }
 bool supported_vt(int vt) { return is_supported_value_type(vt); }
@@ -31,18 +32,38 @@ size_t vec_bytes(int vt) { return vt == BHSP_VALUE_F64 ? 8 : 4; }
 // bytes of one value as the host passes it through the handle API
 size_t host_bytes(int vt) { return vt == BHSP_VALUE_F32 ? 4 : 8; }
 
-bool config_ok(const TileConfig& c) {
-    return (c.seg == 8 || c.seg == 16 || c.seg == 32) && c.tiles_per_worker >= 1 &&
-           c.tiles_per_worker <= (1 << 20) && (c.warps_per_cta == 4 || c.warps_per_cta == 8);
+bool config_ok(const TileConfig& c, int vt) {
+    if (!((c.seg == 8 || c.seg == 16 || c.seg == 32) && c.tiles_per_worker >= 1 &&
+          c.tiles_per_worker <= (1 << 20) && (c.warps_per_cta == 4 || c.warps_per_cta == 8) &&
+          (c.stages == 0 || c.stages == 2 || c.stages == 3)))
+        return false;
+    const int smem = tile_config_smem_bytes(vt, c);
+    return smem >= 0 && smem <= 227 * 1024;
 }
 
-TileConfig make_config(int seg, int tpw, int warps) {
+TileConfig make_config(int seg, int tpw, int warps, int stages) {
     TileConfig c;
     c.seg = seg > 0 ? seg : kDefaultSeg;
     c.tiles_per_worker = tpw > 0 ? tpw : kDefaultTpw;
     c.warps_per_cta = warps > 0 ? warps : kDefaultWarps;
+    c.stages = stages >= 0 ? stages : kDefaultStages;
     return c;
 }
+
+}  // namespace
+
+namespace spmv {
+int tile_config_smem_bytes(int vt, const TileConfig& cfg) {
+    switch (vt) {
+        case BHSP_VALUE_F64: return plain_smem_bytes(true, cfg);
+        case BHSP_VALUE_F32: return plain_smem_bytes(false, cfg);
+        case BHSP_VALUE_MIXED_F32: return mixed_smem_bytes(false, cfg);
+        default: return mixed_smem_bytes(true, cfg);
+    }
+}
+}  // namespace spmv
+
+namespace {
 
 }  // namespace
 
@@ -202,7 +223,8 @@ static int plan_check(bhsp_plan* p, cudaStream_t st) {
 
 extern "C" int bhsp_plan_create(bhsp_plan** out, int value_type, int m, int n, int nnz,
                                 const int* d_row_ptr, const int* d_col_idx, int seg,
-                                int tiles_per_worker, int warps_per_cta, void* stream) {
+                                int tiles_per_worker, int warps_per_cta, int stages,
+                                void* stream) {
     if (!out) return BHSPARSE_INVALID_ARGUMENT;
     *out = nullptr;
     if (!valid_vt(value_type) || !supported_vt(value_type)) return BHSPARSE_UNSUPPORTED_VALUE_TYPE;
@@ -210,8 +232,9 @@ extern "C" int bhsp_plan_create(bhsp_plan** out, int value_type, int m, int n, i
     int rc = check_sizes(m, n, nnz, &msg);
     if (rc) return rc;
     if (!d_row_ptr || (nnz > 0 && !d_col_idx)) return BHSPARSE_INVALID_ARGUMENT;
-    TileConfig cfg = make_config(seg, tiles_per_worker, warps_per_cta);
-    if (!config_ok(cfg)) return BHSPARSE_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(d_col_idx) % 32 != 0) return BHSPARSE_INVALID_ARGUMENT;
+    TileConfig cfg = make_config(seg, tiles_per_worker, warps_per_cta, stages);
+    if (!config_ok(cfg, value_type)) return BHSPARSE_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     rc = validate_on_device(d_row_ptr, d_col_idx, m, n, nnz, st, &msg);
     if (rc) return rc;
@@ -238,6 +261,8 @@ extern "C" int bhsp_plan_execute(bhsp_plan* p, const void* d_val, const void* d_
     if (!p) return BHSPARSE_INVALID_ARGUMENT;
     if (p->m > 0 && (!d_y || (p->nnz > 0 && (!d_val || !d_x))))
         return plan_fail(p, BHSPARSE_INVALID_ARGUMENT, "null device buffer");
+    if (reinterpret_cast<uintptr_t>(d_val) % 32 != 0)
+        return plan_fail(p, BHSPARSE_INVALID_ARGUMENT, "d_val must be 32-byte aligned");
     return plan_execute(p, d_val, d_x, d_y, static_cast<cudaStream_t>(stream));
 }
 
@@ -246,6 +271,8 @@ extern "C" int bhsp_plan_execute_phase(bhsp_plan* p, const void* d_val, const vo
     if (!p || phase < 1 || phase > 3) return BHSPARSE_INVALID_ARGUMENT;
     if (p->m > 0 && (!d_y || (p->nnz > 0 && (!d_val || !d_x))))
         return plan_fail(p, BHSPARSE_INVALID_ARGUMENT, "null device buffer");
+    if (reinterpret_cast<uintptr_t>(d_val) % 32 != 0)
+        return plan_fail(p, BHSPARSE_INVALID_ARGUMENT, "d_val must be 32-byte aligned");
     return plan_execute(p, d_val, d_x, d_y, static_cast<cudaStream_t>(stream), phase);
 }
 
@@ -321,7 +348,7 @@ struct bhsp_spmv {
     int device = 0;
     bool platform = false;
     bool prepared = false;
-    TileConfig cfg = make_config(0, 0, 0);
+    TileConfig cfg = make_config(0, 0, 0, -1);
     int m = 0, n = 0, nnz = 0;
     int* d_row_ptr = nullptr;
     int* d_col = nullptr;
@@ -376,20 +403,22 @@ extern "C" int bhsp_init_platform(bhsp_spmv* h) {
 
 extern "C" int bhsp_free_platform(bhsp_spmv* h) { return h ? BHSPARSE_SUCCESS : BHSPARSE_INVALID_ARGUMENT; }
 
-extern "C" int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int warps_per_cta) {
+extern "C" int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int warps_per_cta,
+                               int stages) {
     if (!h) return BHSPARSE_INVALID_ARGUMENT;
     if (h->prepared) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "set_config after prepare_mem");
-    TileConfig c = make_config(seg, tiles_per_worker, warps_per_cta);
-    if (!config_ok(c)) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "unsupported tile config");
+    TileConfig c = make_config(seg, tiles_per_worker, warps_per_cta, stages);
+    if (!config_ok(c, h->vt)) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "unsupported tile config");
     h->cfg = c;
     return BHSPARSE_SUCCESS;
 }
 
-extern "C" int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tpw, int* warps) {
+extern "C" int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tpw, int* warps, int* stages) {
     if (!h) return BHSPARSE_INVALID_ARGUMENT;
     if (seg) *seg = h->cfg.seg;
     if (tpw) *tpw = h->cfg.tiles_per_worker;
     if (warps) *warps = h->cfg.warps_per_cta;
+    if (stages) *stages = h->cfg.stages;
     return BHSPARSE_SUCCESS;
 }
 
@@ -467,7 +496,7 @@ extern "C" int bhsp_prepare_mem(bhsp_spmv* h, int m, int n, int nnz, const int* 
     if (rc) return rc;
     bhsp_plan* p = nullptr;
     rc = bhsp_plan_create(&p, h->vt, m, n, nnz, h->d_row_ptr, h->d_col, h->cfg.seg,
-                          h->cfg.tiles_per_worker, h->cfg.warps_per_cta, h->stream);
+                          h->cfg.tiles_per_worker, h->cfg.warps_per_cta, h->cfg.stages, h->stream);
     if (rc) {
         handle_release(h);
         h->last_error = rc == BHSPARSE_INVALID_CSR ? "invalid CSR (row_ptr or col_idx)" : "plan creation failed";

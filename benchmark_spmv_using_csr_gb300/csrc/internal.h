@@ -13,6 +13,7 @@ struct TileConfig {
     int seg;               // S in {8, 16, 32}
     int tiles_per_worker;  // >= 1
     int warps_per_cta;     // 4 or 8
+    int stages;            // 0: direct 256-bit loads; 2 or 3: TMA-staged ring of that depth
 };
 
 // partition.cu
@@ -62,5 +63,11 @@ cudaError_t launch_convert_from_f64(const double* src, void* dst, size_t n, bool
 cudaError_t launch_convert_to_f64(const float* src, double* dst, size_t n, cudaStream_t st);
 
 inline bool is_supported_value_type(int vt) { return vt >= 0 && vt <= 3; }
+
+// Dynamic shared memory one CTA of the TMA-staged kernel needs (0 for the direct kernel);
+// value_type as in bhsp_value_type.  Configurations above 227 KB cannot run.
+int tile_config_smem_bytes(int value_type, const TileConfig& cfg);
+int plain_smem_bytes(bool f64, const TileConfig& cfg);
+int mixed_smem_bytes(bool bf16, const TileConfig& cfg);
 
 }  // namespace spmv

@@ -34,19 +34,21 @@ __global__ void k_mark_dirty(const int* __restrict__ row_ptr, int m, int tile, i
     }
 }
 
-// One warp per tile: the raw bit-flag words of every tile, produced by the same
-// tile_flags() the SpMV kernels use (exposed for parity against the reference's words).
+// One warp per tile: the raw bit-flag words of every tile, produced by the same tile_rows()
+// the SpMV kernels use (exposed for parity against the reference's words).
 template <int S>
 __global__ void k_bitflags(const int* __restrict__ row_ptr, int m, int nnz, int ntiles,
                            const uint32_t* __restrict__ tile_ptr, uint32_t* __restrict__ words) {
     __shared__ uint32_t s_words[8][32];
+    __shared__ int s_rowof[8][32 * S];
     const int warp = threadIdx.x >> 5;
     const int t = blockIdx.x * 8 + warp;
     if (t >= ntiles) return;
     const uint32_t tp0 = tile_ptr[t], tp1 = tile_ptr[t + 1];
-    const uint32_t w = tile_flags<S, double>(row_ptr, m, t * 32 * S, (int)(tp0 & ROW_MASK),
-                                             (int)(tp1 & ROW_MASK), false, s_words[warp],
-                                             nullptr, 0, nullptr, nullptr);
+    const int lo = (int)(tp0 & ROW_MASK);
+    const RowBatch rb = prefetch_rows(row_ptr, m, lo);
+    const uint32_t w = tile_rows<S, double>(row_ptr, m, t * 32 * S, lo, (int)(tp1 & ROW_MASK), rb,
+                                            s_words[warp], s_rowof[warp], nullptr);
     words[(size_t)t * 32 + lane_id()] = w;
     (void)nnz;
 }

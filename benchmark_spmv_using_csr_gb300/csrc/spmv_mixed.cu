@@ -4,7 +4,7 @@
 // several tiles or workers in FP64.  No counterpart in the reference, which only has the
 // USE_DOUBLE switch (spmv_cuda/common.h:27-31).
 #include "internal.h"
-#include "tile_kernel.cuh"
+#include "tile_kernel_tma.cuh"
 
 namespace spmv {
 
@@ -60,7 +60,7 @@ cudaError_t launch_mixed(const MixedLaunch& l, const TileConfig& cfg, cudaStream
         a.n = l.n;
         a.nnz = l.nnz;
         a.phase = l.phase;
-        return launch_tiles(a, cfg, st);
+        return launch_tiles_any(a, cfg, st);
     }
     TileArgs<PolMixed<float>> a;
     a.row_ptr = l.row_ptr;
@@ -76,7 +76,11 @@ cudaError_t launch_mixed(const MixedLaunch& l, const TileConfig& cfg, cudaStream
     a.n = l.n;
     a.nnz = l.nnz;
     a.phase = l.phase;
-    return launch_tiles(a, cfg, st);
+    return launch_tiles_any(a, cfg, st);
+}
+
+int mixed_smem_bytes(bool bf16, const TileConfig& cfg) {
+    return bf16 ? tma_smem_bytes<PolMixed<__nv_bfloat16>>(cfg) : tma_smem_bytes<PolMixed<float>>(cfg);
 }
 
 // FP64 -> FP32 or BF16 (round to nearest even), and FP32 -> FP64.

@@ -2,7 +2,7 @@
 // builds, spmv_cuda/common.h:27-31): values, x, y, accumulation and carries all in the
 // value type, one fused multiply-add per non-zero.
 #include "internal.h"
-#include "tile_kernel.cuh"
+#include "tile_kernel_tma.cuh"
 
 namespace spmv {
 
@@ -58,7 +58,7 @@ static cudaError_t launch_plain_any(const PlainLaunch& l, const TileConfig& cfg,
     a.n = l.n;
     a.nnz = l.nnz;
     a.phase = l.phase;
-    return launch_tiles<P>(a, cfg, st);
+    return launch_tiles_any<P>(a, cfg, st);
 }
 
 cudaError_t launch_plain_f64(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st) {
@@ -66,6 +66,10 @@ cudaError_t launch_plain_f64(const PlainLaunch& a, const TileConfig& cfg, cudaSt
 }
 cudaError_t launch_plain_f32(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st) {
     return launch_plain_any<PolF32>(a, cfg, st);
+}
+
+int plain_smem_bytes(bool f64, const TileConfig& cfg) {
+    return f64 ? tma_smem_bytes<PolF64>(cfg) : tma_smem_bytes<PolF32>(cfg);
 }
 
 }  // namespace spmv

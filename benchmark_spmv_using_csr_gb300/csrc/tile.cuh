@@ -31,53 +31,67 @@ __device__ __forceinline__ int search_right(const int* __restrict__ row_ptr, int
     return start;
 }
 
-// Bit-flag word of this lane for tile [e0, e0 + 32*S) whose row span is [lo, hi]
-// (spmv_cuda/kernels_cuda.h:116-148): for every non-empty row r of the span with offset
-// o = row_ptr[r] - e0 in [0, 32*S), bit 31 - o%S of word o/S is set.  The word is in the
-// reference's bit order (slot k of a lane is bit 31-k) and is the raw word, before the
-// reference forces lane 0's head bit (:172).
-//
-// When `dirty` is set the same pass also (a) writes y[r] = 0 for every empty row of the
-// span -- each empty row lies strictly inside exactly one tile span, so it is written once
-// -- and (b) lists the span's non-empty rows in order in s_list, so that the k-th row head
-// of the tile can be mapped to its row.  This is the empty-row calibration of
-// spmv_cuda/bhsparse_spmv_cuda.h:184-222, done at the point where the rows are known
-// instead of by a host pass over a compacted y.
-template <int S, typename VT>
-__device__ __forceinline__ uint32_t tile_flags(const int* __restrict__ row_ptr, int m, int e0,
-                                               int lo, int hi, bool dirty, uint32_t* s_words,
-                                               int* s_list, int list_cap, VT* y,
-                                               uint32_t* err) {
+// First 64 row_ptr entries of a span (two batches of 32 rows, row_ptr[r] and row_ptr[r+1]),
+// loaded one tile ahead of their use.
+struct RowBatch {
+    int a0, b0, a1, b1;
+};
+__device__ __forceinline__ RowBatch prefetch_rows(const int* __restrict__ row_ptr, int m, int lo) {
+    RowBatch rb{0, 0, 0, 0};
+    const int r = lo + lane_id();
+    if (r < m) {
+        rb.a0 = __ldg(row_ptr + r);
+        rb.b0 = __ldg(row_ptr + r + 1);
+    }
+    if (r + 32 < m) {
+        rb.a1 = __ldg(row_ptr + r + 32);
+        rb.b1 = __ldg(row_ptr + r + 33);
+    }
+    return rb;
+}
+
+// Bit-flag word of this lane for tile [e0, e0+32*S) with span [lo, hi] -- the words of
+// spmv_cuda/kernels_cuda.h:116-148: for every non-empty row r of the span whose offset
+// o = row_ptr[r] - e0 lies in [0, 32*S), bit 31 - o%S of word o/S; offsets past the tile are
+// ignored (:131-133) and the word is the raw one, before the reference forces lane 0's head
+// bit (:172) -- plus s_rowof[o] = r for
+// every non-empty row r starting at tile slot o, and y[r] = 0 for every empty row of the
+// span -- each empty row lies strictly inside exactly one span, so it is written once.  The
+// slot -> row map replaces the compacted scatter of kernels_cuda.h:239-257 and the host
+// fix-up of bhsparse_spmv_cuda.h:184-222: a dirty tile writes its rows at their true index.
+template <int S, typename YT>
+__device__ __forceinline__ uint32_t tile_rows(const int* __restrict__ row_ptr, int m, int e0,
+                                              int lo, int hi, const RowBatch& rb,
+                                              uint32_t* s_words, int* s_rowof, YT* y) {
     constexpr int TILE = 32 * S;
     const int lane = lane_id();
     s_words[lane] = 0u;
     __syncwarp();
     const int stop = hi == m ? m - 1 : hi;
-    int nlist = 0;
-    for (int base = lo; base <= stop; base += 32) {
+    for (int base = lo, i = 0; base <= stop; base += 32, ++i) {
         const int r = base + lane;
         const bool valid = r <= stop;
-        int a = 0, b = 0;
+        int A, B;
+        if (i == 0) {
+            A = rb.a0;
+            B = rb.b0;
+        } else if (i == 1) {
+            A = rb.a1;
+            B = rb.b1;
+        } else {
+            A = valid ? __ldg(row_ptr + r) : 0;
+            B = valid ? __ldg(row_ptr + r + 1) : 0;
+        }
         if (valid) {
-            a = __ldg(row_ptr + r);
-            b = __ldg(row_ptr + r + 1);
-        }
-        const bool nonempty = valid && a != b;
-        if (nonempty) {
-            const int off = a - e0;
-            if (off >= 0 && off < TILE) atomicOr(&s_words[off / S], 1u << (31 - off % S));
-        }
-        if (dirty) {
-            if (valid && !nonempty && y != nullptr) y[r] = VT(0);
-            const uint32_t bal = __ballot_sync(SPMV_FULL_MASK, nonempty);
-            if (nonempty && s_list != nullptr) {
-                const int idx = nlist + __popc(bal & ((1u << lane) - 1u));
-                if (idx < list_cap)
-                    s_list[idx] = r;
-                else if (err)
-                    atomicOr(err, ERR_LIST_OVERFLOW);
+            if (A != B) {
+                const int off = A - e0;
+                if (off >= 0 && off < TILE) {
+                    atomicOr(&s_words[off / S], 1u << (31 - off % S));
+                    s_rowof[off] = r;
+                }
+            } else if (y != nullptr) {
+                y[r] = YT(0);
             }
-            nlist += __popc(bal);
         }
     }
     __syncwarp();

@@ -67,75 +67,9 @@ __device__ __forceinline__ float2 sh_xor(float2 v, int d) {
     return make_float2(__shfl_xor_sync(SPMV_FULL_MASK, v.x, d), __shfl_xor_sync(SPMV_FULL_MASK, v.y, d));
 }
 
-// ---- streamed loads of 8 consecutive non-zeros of one lane ----
-__device__ __forceinline__ void load8_full(const double* val, const int* col, int e, uint64_t pol,
-                                           double (&v)[8], int (&c)[8]) {
-    double a[4], b[4];
-    uint32_t cc[8];
-    ld_stream_f64x4(val + e, pol, a);
-    ld_stream_f64x4(val + e + 4, pol, b);
-    ld_stream_b32x8(col + e, pol, cc);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        v[i] = a[i];
-        v[i + 4] = b[i];
-    }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) c[i] = (int)cc[i];
-}
-__device__ __forceinline__ void load8_full(const float* val, const int* col, int e, uint64_t pol,
-                                           float (&v)[8], int (&c)[8]) {
-    uint32_t vv[8], cc[8];
-    ld_stream_b32x8(val + e, pol, vv);
-    ld_stream_b32x8(col + e, pol, cc);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        v[i] = __uint_as_float(vv[i]);
-        c[i] = (int)cc[i];
-    }
-}
-__device__ __forceinline__ void load8_full(const __nv_bfloat16* val, const int* col, int e,
-                                           uint64_t pol, float (&v)[8], int (&c)[8]) {
-    uint32_t vv[4], cc[8];
-    ld_stream_b32x4(val + e, pol, vv);
-    ld_stream_b32x8(col + e, pol, cc);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        v[2 * i] = __uint_as_float(vv[i] << 16);          // low half = element 2i
-        v[2 * i + 1] = __uint_as_float(vv[i] & 0xffff0000u);
-    }
-#pragma unroll
-    for (int i = 0; i < 8; ++i) c[i] = (int)cc[i];
-}
 __device__ __forceinline__ double to_compute(double v) { return v; }
 __device__ __forceinline__ float to_compute(float v) { return v; }
 __device__ __forceinline__ float to_compute(__nv_bfloat16 v) { return __bfloat162float(v); }
-
-template <typename VS, typename VC>
-__device__ __forceinline__ void load8_tail(const VS* val, const int* col, int e, int nnz,
-                                           VC (&v)[8], int (&c)[8]) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        if (e + i < nnz) {
-            v[i] = to_compute(val[e + i]);
-            c[i] = col[e + i];
-        } else {
-            v[i] = VC(0);
-            c[i] = -1;  // padding slot: contributes 0, x is not read
-        }
-    }
-}
-
-template <class P, int S>
-__device__ __forceinline__ void load_chunk(const TileArgs<P>& a, int t, int c, int lane,
-                                           uint64_t pol, typename P::VC (&v)[8], int (&cc)[8]) {
-    constexpr int TILE = 32 * S;
-    const int e = t * TILE + lane * S + c * 8;
-    if ((long long)(t + 1) * TILE <= a.nnz)
-        load8_full(a.val, a.col, e, pol, v, cc);
-    else
-        load8_tail(a.val, a.col, e, a.nnz, v, cc);
-}
 
 template <typename XT>
 __device__ __forceinline__ void gather8(const XT* __restrict__ x, const int (&c)[8], uint64_t pol,
@@ -144,15 +78,6 @@ __device__ __forceinline__ void gather8(const XT* __restrict__ x, const int (&c)
     for (int i = 0; i < 8; ++i) xv[i] = c[i] >= 0 ? ld_x(x + c[i], pol) : XT(0);
 }
 
-// Row of the q-th non-empty row of the span (checked: a bad index is recorded in the error
-// word and yields -1, whose store is then skipped).
-__device__ __forceinline__ int span_row(bool dirty, const int* list, int lo, int q, int cap,
-                                        uint32_t* err) {
-    if (!dirty) return lo + q;
-    if ((unsigned)q < (unsigned)cap) return list[q];
-    atomicOr(err, ERR_LIST_OVERFLOW);
-    return -1;
-}
 template <typename YT>
 __device__ __forceinline__ void store_row(YT* y, int m, int row, YT v, uint32_t* err) {
     if ((unsigned)row < (unsigned)m)
@@ -168,6 +93,67 @@ __device__ __forceinline__ typename P::Acc warp_sum_acc(typename P::Acc v) {
     return v;
 }
 
+// Column indices / values of chunk c (8 non-zeros) of tile t for this lane.
+template <class P, int S>
+__device__ __forceinline__ void load_cols(const TileArgs<P>& a, int t, int c, int lane,
+                                          uint64_t pol, int (&cc)[8]) {
+    constexpr int TILE = 32 * S;
+    const int e = t * TILE + lane * S + c * 8;
+    if ((long long)(t + 1) * TILE <= a.nnz) {
+        uint32_t u[8];
+        ld_stream_b32x8(a.col + e, pol, u);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) cc[i] = (int)u[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) cc[i] = e + i < a.nnz ? a.col[e + i] : -1;
+    }
+}
+__device__ __forceinline__ void load_vals8(const double* val, int e, uint64_t pol, double (&v)[8]) {
+    double p[4], q[4];
+    ld_stream_f64x4(val + e, pol, p);
+    ld_stream_f64x4(val + e + 4, pol, q);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        v[i] = p[i];
+        v[i + 4] = q[i];
+    }
+}
+__device__ __forceinline__ void load_vals8(const float* val, int e, uint64_t pol, float (&v)[8]) {
+    uint32_t u[8];
+    ld_stream_b32x8(val + e, pol, u);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(u[i]);
+}
+__device__ __forceinline__ void load_vals8(const __nv_bfloat16* val, int e, uint64_t pol,
+                                           float (&v)[8]) {
+    uint32_t u[4];
+    ld_stream_b32x4(val + e, pol, u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        v[2 * i] = __uint_as_float(u[i] << 16);  // the low half holds element 2i
+        v[2 * i + 1] = __uint_as_float(u[i] & 0xffff0000u);
+    }
+}
+template <class P, int S>
+__device__ __forceinline__ void load_vals(const TileArgs<P>& a, int t, int c, int lane,
+                                          uint64_t pol, typename P::VC (&v)[8]) {
+    constexpr int TILE = 32 * S;
+    const int e = t * TILE + lane * S + c * 8;
+    if ((long long)(t + 1) * TILE <= a.nnz) {
+        load_vals8(a.val, e, pol, v);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            v[i] = e + i < a.nnz ? to_compute(a.val[e + i]) : typename P::VC(0);
+    }
+}
+
+// The tile kernel.  One warp = one worker over tiles [t_begin, t_end).  The stream runs as a
+// software pipeline over the worker's chunks of 8 non-zeros per lane: while chunk g is
+// multiplied, the values of chunk g+1 and the column indices of chunk g+2 are in flight and the
+// x gathers of chunk g+1 are issued; the bit flags' row_ptr entries and tile_ptr are fetched
+// one tile ahead.
 template <class P, int S, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32)
     k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
@@ -178,9 +164,8 @@ __global__ void __launch_bounds__(WARPS * 32)
     using YT = typename P::YT;
     constexpr int TILE = 32 * S;
     constexpr int NC = S / 8;
-    constexpr int LIST = TILE + 1;  // non-empty rows of one tile span: at most TILE + 1
     __shared__ uint32_t s_words[WARPS][32];
-    __shared__ int s_list[WARPS][LIST];
+    __shared__ int s_rowof[WARPS][TILE];
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -190,7 +175,25 @@ __global__ void __launch_bounds__(WARPS * 32)
     const int t_end = min(t_begin + tpw, ntiles);
     const uint64_t pol_s = policy_evict_first();
     const uint64_t pol_x = policy_evict_last();
-    int* const list = s_list[warp];
+    int* const rowof = s_rowof[warp];
+
+    uint32_t tp0 = __ldg(a.tile_ptr + t_begin);
+    uint32_t tp1 = __ldg(a.tile_ptr + t_begin + 1);
+    RowBatch rb = prefetch_rows(a.row_ptr, a.m, (int)(tp0 & ROW_MASK));
+
+    // pipeline registers: A = chunk g (values, x) and g+1 (columns); B = the next ones
+    int colA[8], colB[8];
+    VC valA[8], valB[8];
+    XT xA[8], xB[8];
+    {
+        int col0[8];
+        load_cols<P, S>(a, t_begin, 0, lane, pol_s, col0);
+        load_vals<P, S>(a, t_begin, 0, lane, pol_s, valA);
+        gather8(a.x, col0, pol_x, xA);
+        const int t1 = t_begin + (NC > 1 ? 0 : 1);
+        const int c1 = NC > 1 ? 1 : 0;
+        if (t1 < t_end) load_cols<P, S>(a, t1, c1, lane, pol_s, colA);
+    }
 
     int carry_row = -1;  // row of the segment left open by the previous tile (-1: none)
     bool carry_owned = false;
@@ -198,7 +201,6 @@ __global__ void __launch_bounds__(WARPS * 32)
     Acc dc = P::zero();  // per-lane partials of carry_row from tiles without a row head
     bool dc_active = false;
     bool rec_written = false;
-
     auto flush = [&](int row, Carry v, bool owned) {
         if (lane == 0) {
             if (owned) {
@@ -211,23 +213,19 @@ __global__ void __launch_bounds__(WARPS * 32)
         if (!owned) rec_written = true;
     };
 
-    VC cv[8], nv[8];
-    XT xv[8];
-    int cc[8], nc[8];
-    load_chunk<P, S>(a, t_begin, 0, lane, pol_s, cv, cc);
-
     for (int t = t_begin; t < t_end; ++t) {
-        const uint32_t tp0 = __ldg(a.tile_ptr + t);
-        const uint32_t tp1 = __ldg(a.tile_ptr + t + 1);
         const int lo = (int)(tp0 & ROW_MASK);
         const int hi = (int)(tp1 & ROW_MASK);
-        const bool dirty = (tp0 & DIRTY_BIT) != 0u;
-        const int e0 = t * TILE;
-        const uint32_t w = tile_flags<S, YT>(a.row_ptr, a.m, e0, lo, hi, dirty, s_words[warp],
-                                             list, LIST, a.y, a.err);
-        const bool first_head = ((shfl_idx(w, 0) >> 31) & 1u) != 0u;
-        const int nf = __popc(w);
-        const uint32_t fmask = __ballot_sync(SPMV_FULL_MASK, nf > 0);
+        uint32_t tp2 = 0u;
+        RowBatch rbn{0, 0, 0, 0};
+        if (t + 1 < t_end) {  // the next tile's meta, one tile ahead
+            tp2 = __ldg(a.tile_ptr + t + 2);
+            rbn = prefetch_rows(a.row_ptr, a.m, hi);
+        }
+        const uint32_t w = tile_rows<S, YT>(a.row_ptr, a.m, t * TILE, lo, hi, rb, s_words[warp],
+                                            rowof, a.y);
+        const bool first_head = ((__shfl_sync(SPMV_FULL_MASK, w, 0) >> 31) & 1u) != 0u;
+        const uint32_t fmask = __ballot_sync(SPMV_FULL_MASK, w != 0u);
 
         if (first_head) {
             // the open row ended exactly at this tile's start
@@ -246,69 +244,57 @@ __global__ void __launch_bounds__(WARPS * 32)
             carry_owned = false;
             carry = P::carry_zero();
         }
-
-        if (fmask == 0u) {
-            // no row head anywhere in the tile: every slot continues carry_row
-            Acc r = dc;
-#pragma unroll
-            for (int c = 0; c < NC; ++c) {
-                if (c + 1 < NC)
-                    load_chunk<P, S>(a, t, c + 1, lane, pol_s, nv, nc);
-                else if (t + 1 < t_end)
-                    load_chunk<P, S>(a, t + 1, 0, lane, pol_s, nv, nc);
-                gather8(a.x, cc, pol_x, xv);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) r = P::fma(cv[k], xv[k], r);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    cv[k] = nv[k];
-                    cc[k] = nc[k];
-                }
-            }
-            dc = r;
-            dc_active = true;
-            continue;
-        }
-        if (dc_active) {
+        if (fmask != 0u && dc_active) {
             carry = P::carry_add(carry, warp_sum_acc<P>(dc));
             dc = P::zero();
             dc_active = false;
         }
 
-        // ordinal (among the span's non-empty rows) of this lane's first row head
-        const int qbase = warp_exclusive_scan(nf) + (first_head ? 0 : 1);
-        Acc run = P::zero(), head = P::zero();
-        int fidx = 0;
+        Acc run = fmask ? P::zero() : dc;
+        Acc head = P::zero();
+        int cur_row = -1;  // row of this lane's open segment
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
-            if (c + 1 < NC)
-                load_chunk<P, S>(a, t, c + 1, lane, pol_s, nv, nc);
-            else if (t + 1 < t_end)
-                load_chunk<P, S>(a, t + 1, 0, lane, pol_s, nv, nc);
-            gather8(a.x, cc, pol_x, xv);
+            // issue: columns of chunk g+2, values and x of chunk g+1
+            const int t1 = t + (c + 1) / NC, c1 = (c + 1) % NC;
+            const int t2 = t + (c + 2) / NC, c2 = (c + 2) % NC;
+            if (t2 < t_end) load_cols<P, S>(a, t2, c2, lane, pol_s, colB);
+            if (t1 < t_end) {
+                load_vals<P, S>(a, t1, c1, lane, pol_s, valB);
+                gather8(a.x, colA, pol_x, xB);
+            }
+            // multiply chunk g
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                const bool f = ((w >> (31 - (c * 8 + k))) & 1u) != 0u;
-                if (f) {
-                    if (fidx > 0) {  // a row that starts and ends inside this lane
-                        const int row = span_row(dirty, list, lo, qbase + fidx - 1, LIST, a.err);
-                        store_row(a.y, a.m, row, P::out_acc(run), a.err);
-                    } else {
+                const int kk = c * 8 + k;
+                if ((w >> (31 - kk)) & 1u) {
+                    if (cur_row >= 0)
+                        store_row(a.y, a.m, cur_row, P::out_acc(run), a.err);  // complete in lane
+                    else
                         head = run;  // slots before the lane's first row head
-                    }
-                    ++fidx;
+                    cur_row = rowof[lane * S + kk];
                     run = P::zero();
                 }
-                run = P::fma(cv[k], xv[k], run);
+                run = P::fma(valA[k], xA[k], run);
             }
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                cv[k] = nv[k];
-                cc[k] = nc[k];
+                colA[k] = colB[k];
+                valA[k] = valB[k];
+                xA[k] = xB[k];
             }
         }
+        __syncwarp();  // rowof / s_words are rebuilt by the next tile
 
-        const bool has = fidx > 0;
+        tp0 = tp1;
+        tp1 = tp2;
+        rb = rbn;
+        if (fmask == 0u) {  // no row head: the whole tile continues carry_row
+            dc = run;
+            dc_active = true;
+            continue;
+        }
+        const bool has = cur_row >= 0;
         if (!has) head = run;
         // T_l = head_l + (has_l ? 0 : T_{l+1}): the head-less run that starts at lane l
         Acc T = head;
@@ -339,15 +325,12 @@ __global__ void __launch_bounds__(WARPS * 32)
         const Acc T0 = sh_idx(T, 0);
         const int last = 31 - __clz(fmask);
         Acc fin = P::zero();
-        int frow = 0;
         if (has) {
             fin = P::add(run, A);
-            frow = span_row(dirty, list, lo, qbase + fidx - 1, LIST, a.err);
-            if (lane != last) store_row(a.y, a.m, frow, P::out_acc(fin), a.err);
+            if (lane != last) store_row(a.y, a.m, cur_row, P::out_acc(fin), a.err);
         }
-        if (!first_head) flush(carry_row, P::carry_add(carry, T0), carry_owned);  // open row ends here
-        carry_row = __shfl_sync(SPMV_FULL_MASK, frow, last);
-        if (carry_row < 0) carry_row = -1;  // a failed lookup was recorded; nothing to carry
+        if (!first_head) flush(carry_row, P::carry_add(carry, T0), carry_owned);  // open row ends
+        carry_row = __shfl_sync(SPMV_FULL_MASK, cur_row, last);
         carry = P::carry_from(sh_idx(fin, last));
         carry_owned = true;
     }

@@ -82,9 +82,13 @@ const char* bhsp_last_error(const bhsp_spmv* h);
 /* Choose the CUDA device used by init_platform (default 0, as the reference hard-codes). */
 int bhsp_set_device(bhsp_spmv* h, int device);
 /* Tile schedule: seg = non-zeros per lane (8, 16 or 32), tiles_per_worker >= 1,
- * warps_per_cta 4 or 8.  Before prepare_mem; 0 for any field keeps the default. */
-int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int warps_per_cta);
-int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tiles_per_worker, int* warps_per_cta);
+ * warps_per_cta 4 or 8, stages = 0 (each lane streams its values with 256-bit loads) or 2 / 3
+ * (values and column indices staged in a shared-memory ring of that many tiles by bulk
+ * copies).  Before prepare_mem; 0 for seg / tiles_per_worker / warps_per_cta and -1 for
+ * stages keep the default.  Rejected if the staged ring does not fit in shared memory. */
+int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int warps_per_cta, int stages);
+int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tiles_per_worker, int* warps_per_cta,
+                    int* stages);
 /* Replace x (host pointer, same type as in prepare_mem) without rebuilding anything. */
 int bhsp_set_x(bhsp_spmv* h, const void* x);
 /* Enqueue y = A.x on `stream` (a cudaStream_t, NULL = the legacy default stream) and
@@ -107,13 +111,14 @@ size_t bhsp_device_bytes(const bhsp_spmv* h);
 typedef struct bhsp_plan bhsp_plan;
 
 /* Validates the CSR on the device, builds tile_ptr and allocates the carry records.
- * row_ptr / col_idx stay owned by the caller and must outlive the plan.
- * seg / tiles_per_worker / warps_per_cta as in bhsp_set_config (0 = default). */
+ * row_ptr / col_idx stay owned by the caller and must outlive the plan; col_idx must be
+ * 32-byte aligned.  The schedule fields are as in bhsp_set_config. */
 int bhsp_plan_create(bhsp_plan** out, int value_type, int m, int n, int nnz,
                      const int* d_row_ptr, const int* d_col_idx, int seg, int tiles_per_worker,
-                     int warps_per_cta, void* stream);
+                     int warps_per_cta, int stages, void* stream);
 /* y = A.x, enqueued on `stream`.  d_val in the storage type of value_type (double, float,
- * float, __nv_bfloat16), d_x / d_y in the x/y type (double for F64, float otherwise). */
+ * float, __nv_bfloat16), 32-byte aligned; d_x / d_y in the x/y type (double for F64, float
+ * otherwise). */
 int bhsp_plan_execute(bhsp_plan* p, const void* d_val, const void* d_x, void* d_y, void* stream);
 /* One phase of bhsp_plan_execute (1 = tile kernel, 2 = calibration, 3 = both). */
 int bhsp_plan_execute_phase(bhsp_plan* p, const void* d_val, const void* d_x, void* d_y,

@@ -51,11 +51,15 @@ def test_config_validation_without_gpu():
     s = sp.BhsparseSpmvCuda(sp.VALUE_F64)
     assert s.get_config() == sp.DEFAULT_CONFIG
     assert s.set_config(12, 1, 4) == sp.BHSPARSE_INVALID_ARGUMENT
-    assert s.set_config(16, 2, 4) == sp.BHSPARSE_SUCCESS
-    assert s.get_config() == (16, 2, 4)
-    assert s.set_config(8, 0, 0) == sp.BHSPARSE_SUCCESS
-    assert s.get_config() == (8, 4, 8)
+    assert s.set_config(16, 2, 4, 0) == sp.BHSPARSE_SUCCESS
+    assert s.get_config() == (16, 2, 4, 0)
+    assert s.set_config(8, 0, 0, -1) == sp.BHSPARSE_SUCCESS
+    assert s.get_config() == (8,) + sp.DEFAULT_CONFIG[1:]
     assert s.set_config(8, 1, 6) == sp.BHSPARSE_INVALID_ARGUMENT
+    assert s.set_config(8, 1, 4, 1) == sp.BHSPARSE_INVALID_ARGUMENT
+    assert s.set_config(16, 4, 8, 3) == sp.BHSPARSE_SUCCESS  # 8 warps x 3 FP64 slots fit
+    # 8 warps x 3 slots of 32 x 32 FP64 runs exceed 227 KB of shared memory
+    assert s.set_config(32, 4, 8, 3) == sp.BHSPARSE_INVALID_ARGUMENT
     s.close()
 
 

@@ -16,8 +16,10 @@ from benchmark_spmv_using_csr_gb300 import gen
 
 pytestmark = pytest.mark.gpu
 
-CONFIGS = [(8, 1, 4), (8, 3, 8), (16, 1, 8), (16, 5, 4), (32, 1, 4), (32, 2, 8), (32, 4, 8),
-           (32, 9, 4)]
+# (non-zeros per lane, tiles per worker, warps per CTA, stages): direct loads (0 stages) and
+# the TMA-staged ring (2 or 3 stages)
+CONFIGS = [(8, 1, 4, 0), (8, 3, 8, 0), (16, 1, 8, 0), (16, 5, 4, 0), (32, 1, 4, 0), (32, 9, 4, 0),
+           (8, 1, 4, 2), (8, 7, 8, 3), (16, 2, 4, 3), (16, 4, 8, 2), (32, 3, 4, 2), (32, 1, 4, 3)]
 
 
 def run_handle(vt, rp, col, val, x, cfg=None, y0=None, repeat=1):
@@ -54,6 +56,22 @@ def int_csr(rng, m=None, n=None, maxlen=None, empty=None):
     val = rng.integers(-9, 10, int(rp[-1])).astype(np.float64)
     x = rng.integers(-9, 10, n).astype(np.float64)
     return rp, col, val, x
+
+
+MIXED_CONFIGS = [(16, 4, 4, 0), (8, 3, 8, 2), (16, 2, 4, 3), (32, 1, 4, 2)]
+
+
+@pytest.mark.parametrize("cfg", MIXED_CONFIGS)
+def test_mixed_forms_configs(cuda_ok, cfg):
+    rng = np.random.default_rng(77)
+    a, x = _real_case(rng, "powerlaw")
+    ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)
+    y = run_handle(sp.VALUE_MIXED_F32, a.row_ptr, a.col, a.val, x, cfg)
+    assert oracle.normwise_error(y, ystar) <= TOL_MIXED_NORMWISE
+    yb = run_handle(sp.VALUE_MIXED_BF16, a.row_ptr, a.col, a.val, x, cfg)
+    ystar_b = oracle.csr_dot2(a.row_ptr, a.col, bf16_round(a.val),
+                              x.astype(np.float32).astype(np.float64))
+    assert oracle.normwise_error(yb, ystar_b) <= TOL_MIXED_NORMWISE
 
 
 def test_known_6x6_all_forms(cuda_ok):
@@ -94,7 +112,7 @@ def test_y_contents_and_repeated_calls(cuda_ok):
     rng = np.random.default_rng(5)
     rp, col, val, x = int_csr(rng, m=5000, maxlen=80, empty=0.1)
     yr = oracle.csr_serial(rp, col, val, x)
-    y = run_handle(sp.VALUE_F64, rp, col, val, x, (8, 1, 4), y0=np.full(5000, 7.5), repeat=5)
+    y = run_handle(sp.VALUE_F64, rp, col, val, x, (8, 1, 4, 2), y0=np.full(5000, 7.5), repeat=5)
     assert np.array_equal(y, yr)
 
 
@@ -152,10 +170,10 @@ def test_mixed_forms_normwise(cuda_ok, kind):
     rng = np.random.default_rng(200 + KINDS.index(kind))
     a, x = _real_case(rng, kind)
     ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)
-    y = run_handle(sp.VALUE_MIXED_F32, a.row_ptr, a.col, a.val, x, (32, 4, 8))
+    y = run_handle(sp.VALUE_MIXED_F32, a.row_ptr, a.col, a.val, x, (16, 4, 4, 0))
     assert oracle.normwise_error(y, ystar) <= TOL_MIXED_NORMWISE
     # BF16 storage: the arithmetic is judged against y* of the BF16-rounded values and FP32 x
-    yb = run_handle(sp.VALUE_MIXED_BF16, a.row_ptr, a.col, a.val, x, (32, 4, 8))
+    yb = run_handle(sp.VALUE_MIXED_BF16, a.row_ptr, a.col, a.val, x, (16, 4, 4, 3))
     ystar_b = oracle.csr_dot2(a.row_ptr, a.col, bf16_round(a.val),
                               x.astype(np.float32).astype(np.float64))
     assert oracle.normwise_error(yb, ystar_b) <= TOL_MIXED_NORMWISE
