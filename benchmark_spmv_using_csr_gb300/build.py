@@ -23,6 +23,8 @@ LIB_PATH = os.path.join(HERE, LIB_NAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp,-O3",
                      "--expt-relaxed-constexpr", "-I" + INCLUDE]
+# extra -D flags for experiments (e.g. SPMV_NVCC_DEFINES="-DSPMV_CACHE_MODE=1")
+NVCC_FLAGS += os.environ.get("SPMV_NVCC_DEFINES", "").split()
 LINK_FLAGS = ["-shared", "-Xcompiler", "-fopenmp", "-lgomp"]
 
 

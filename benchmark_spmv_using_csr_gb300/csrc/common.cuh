@@ -82,34 +82,112 @@ __device__ __forceinline__ uint64_t policy_evict_last() {
     return p;
 }
 
+// Cache treatment of the two access streams (compile-time):
+//   1: no L2 policy on either (the val / col stream skips L1 allocation) -- the default: on
+//      GB300 it is the fastest on both benchmark matrices (27-point stencil +6 % over 0)
+//   0: val/col stream with an L2 evict-first policy, x gathers with an L2 evict-last policy
+//   2: evict-first on the stream only
+//   3: as 0, plus a 256-byte L2 prefetch hint on the stream
+#ifndef SPMV_CACHE_MODE
+#define SPMV_CACHE_MODE 1
+#endif
+#if SPMV_CACHE_MODE == 1
+#define SPMV_STREAM_HINT ""
+#elif SPMV_CACHE_MODE == 3
+#define SPMV_STREAM_HINT ".L2::cache_hint.L2::256B"
+#else
+#define SPMV_STREAM_HINT ".L2::cache_hint"
+#endif
+#if SPMV_CACHE_MODE == 1 || SPMV_CACHE_MODE == 2
+#define SPMV_X_HINT ""
+#else
+#define SPMV_X_HINT ".L2::cache_hint"
+#endif
+
 // ---- 256-bit streaming loads (address must be 32-byte aligned) ----
 __device__ __forceinline__ void ld_stream_f64x4(const double* p, uint64_t pol, double (&v)[4]) {
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f64 {%0,%1,%2,%3}, [%4], %5;"
+#if SPMV_CACHE_MODE == 1
+    (void)pol;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.f64 {%0,%1,%2,%3}, [%4];"
+                 : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3])
+                 : "l"(p));
+#else
+    asm volatile("ld.global.nc.L1::no_allocate" SPMV_STREAM_HINT ".v4.f64 {%0,%1,%2,%3}, [%4], %5;"
                  : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3])
                  : "l"(p), "l"(pol));
+#endif
 }
 __device__ __forceinline__ void ld_stream_b32x8(const void* p, uint64_t pol, uint32_t (&v)[8]) {
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+#if SPMV_CACHE_MODE == 1
+    (void)pol;
+    asm volatile("ld.global.nc.L1::no_allocate.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                   "=r"(v[7])
+                 : "l"(p));
+#else
+    asm volatile("ld.global.nc.L1::no_allocate" SPMV_STREAM_HINT
+                 ".v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
                  : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
                    "=r"(v[7])
                  : "l"(p), "l"(pol));
+#endif
 }
 // 128-bit streaming load (16-byte aligned)
 __device__ __forceinline__ void ld_stream_b32x4(const void* p, uint64_t pol, uint32_t (&v)[4]) {
-    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.b32 {%0,%1,%2,%3}, [%4], %5;"
+#if SPMV_CACHE_MODE == 1
+    (void)pol;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+                 : "l"(p));
+#else
+    asm volatile("ld.global.nc.L1::no_allocate" SPMV_STREAM_HINT ".v4.b32 {%0,%1,%2,%3}, [%4], %5;"
                  : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
                  : "l"(p), "l"(pol));
+#endif
+}
+
+// 64-bit streaming load (8-byte aligned)
+__device__ __forceinline__ void ld_stream_b32x2(const void* p, uint64_t pol, uint32_t (&v)[2]) {
+#if SPMV_CACHE_MODE == 1
+    (void)pol;
+    asm volatile("ld.global.nc.L1::no_allocate.v2.b32 {%0,%1}, [%2];" : "=r"(v[0]), "=r"(v[1]) : "l"(p));
+#else
+    asm volatile("ld.global.nc.L1::no_allocate" SPMV_STREAM_HINT ".v2.b32 {%0,%1}, [%2], %3;"
+                 : "=r"(v[0]), "=r"(v[1])
+                 : "l"(p), "l"(pol));
+#endif
+}
+
+// N consecutive 32-bit words with one vector load (N = 2, 4 or 8)
+__device__ __forceinline__ void ld_stream_u32s(const void* p, uint64_t pol, uint32_t (&v)[8]) {
+    ld_stream_b32x8(p, pol, v);
+}
+__device__ __forceinline__ void ld_stream_u32s(const void* p, uint64_t pol, uint32_t (&v)[4]) {
+    ld_stream_b32x4(p, pol, v);
+}
+__device__ __forceinline__ void ld_stream_u32s(const void* p, uint64_t pol, uint32_t (&v)[2]) {
+    ld_stream_b32x2(p, pol, v);
 }
 
 // ---- x gathers: read-only path, kept in L2 ----
 __device__ __forceinline__ double ld_x(const double* p, uint64_t pol) {
     double v;
+#if SPMV_CACHE_MODE == 1 || SPMV_CACHE_MODE == 2
+    (void)pol;
+    asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+#else
     asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+#endif
     return v;
 }
 __device__ __forceinline__ float ld_x(const float* p, uint64_t pol) {
     float v;
+#if SPMV_CACHE_MODE == 1 || SPMV_CACHE_MODE == 2
+    (void)pol;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+#else
     asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+#endif
     return v;
 }
 

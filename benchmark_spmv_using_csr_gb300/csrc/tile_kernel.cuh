@@ -71,11 +71,18 @@ __device__ __forceinline__ double to_compute(double v) { return v; }
 __device__ __forceinline__ float to_compute(float v) { return v; }
 __device__ __forceinline__ float to_compute(__nv_bfloat16 v) { return __bfloat162float(v); }
 
-template <typename XT>
-__device__ __forceinline__ void gather8(const XT* __restrict__ x, const int (&c)[8], uint64_t pol,
-                                        XT (&xv)[8]) {
+// Non-zeros per lane handled per pipeline step (a "chunk"): 4 for S = 8 (two steps per tile,
+// fewer live registers), 8 otherwise.
+template <int S>
+constexpr int chunk_width() {
+    return S == 8 ? 4 : 8;
+}
+
+template <int CW, typename XT>
+__device__ __forceinline__ void gather_cw(const XT* __restrict__ x, const int (&c)[CW], uint64_t pol,
+                                          XT (&xv)[CW]) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) xv[i] = c[i] >= 0 ? ld_x(x + c[i], pol) : XT(0);
+    for (int i = 0; i < CW; ++i) xv[i] = c[i] >= 0 ? ld_x(x + c[i], pol) : XT(0);
 }
 
 template <typename YT>
@@ -93,64 +100,70 @@ __device__ __forceinline__ typename P::Acc warp_sum_acc(typename P::Acc v) {
     return v;
 }
 
-// Column indices / values of chunk c (8 non-zeros) of tile t for this lane.
-template <class P, int S>
+// Column indices / values of chunk c (CW non-zeros) of tile t for this lane: one vector load
+// each on full tiles, guarded scalar loads on the matrix's last, partial tile (column -1 and
+// value 0 mark padding slots, which contribute nothing and read no x).
+template <class P, int S, int CW>
 __device__ __forceinline__ void load_cols(const TileArgs<P>& a, int t, int c, int lane,
-                                          uint64_t pol, int (&cc)[8]) {
+                                          uint64_t pol, int (&cc)[CW]) {
     constexpr int TILE = 32 * S;
-    const int e = t * TILE + lane * S + c * 8;
+    const int e = t * TILE + lane * S + c * CW;
     if ((long long)(t + 1) * TILE <= a.nnz) {
-        uint32_t u[8];
-        ld_stream_b32x8(a.col + e, pol, u);
+        uint32_t u[CW];
+        ld_stream_u32s(a.col + e, pol, u);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) cc[i] = (int)u[i];
+        for (int i = 0; i < CW; ++i) cc[i] = (int)u[i];
     } else {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) cc[i] = e + i < a.nnz ? a.col[e + i] : -1;
+        for (int i = 0; i < CW; ++i) cc[i] = e + i < a.nnz ? a.col[e + i] : -1;
     }
 }
-__device__ __forceinline__ void load_vals8(const double* val, int e, uint64_t pol, double (&v)[8]) {
-    double p[4], q[4];
-    ld_stream_f64x4(val + e, pol, p);
-    ld_stream_f64x4(val + e + 4, pol, q);
+template <int CW>
+__device__ __forceinline__ void load_vals_full(const double* val, int e, uint64_t pol,
+                                               double (&v)[CW]) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        v[i] = p[i];
-        v[i + 4] = q[i];
+    for (int h = 0; h < CW / 4; ++h) {
+        double p[4];
+        ld_stream_f64x4(val + e + 4 * h, pol, p);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) v[4 * h + i] = p[i];
     }
 }
-__device__ __forceinline__ void load_vals8(const float* val, int e, uint64_t pol, float (&v)[8]) {
-    uint32_t u[8];
-    ld_stream_b32x8(val + e, pol, u);
+template <int CW>
+__device__ __forceinline__ void load_vals_full(const float* val, int e, uint64_t pol,
+                                               float (&v)[CW]) {
+    uint32_t u[CW];
+    ld_stream_u32s(val + e, pol, u);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(u[i]);
+    for (int i = 0; i < CW; ++i) v[i] = __uint_as_float(u[i]);
 }
-__device__ __forceinline__ void load_vals8(const __nv_bfloat16* val, int e, uint64_t pol,
-                                           float (&v)[8]) {
-    uint32_t u[4];
-    ld_stream_b32x4(val + e, pol, u);
+template <int CW>
+__device__ __forceinline__ void load_vals_full(const __nv_bfloat16* val, int e, uint64_t pol,
+                                               float (&v)[CW]) {
+    uint32_t u[CW / 2];
+    ld_stream_u32s(val + e, pol, u);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < CW / 2; ++i) {
         v[2 * i] = __uint_as_float(u[i] << 16);  // the low half holds element 2i
         v[2 * i + 1] = __uint_as_float(u[i] & 0xffff0000u);
     }
 }
-template <class P, int S>
+template <class P, int S, int CW>
 __device__ __forceinline__ void load_vals(const TileArgs<P>& a, int t, int c, int lane,
-                                          uint64_t pol, typename P::VC (&v)[8]) {
+                                          uint64_t pol, typename P::VC (&v)[CW]) {
     constexpr int TILE = 32 * S;
-    const int e = t * TILE + lane * S + c * 8;
+    const int e = t * TILE + lane * S + c * CW;
     if ((long long)(t + 1) * TILE <= a.nnz) {
-        load_vals8(a.val, e, pol, v);
+        load_vals_full(a.val, e, pol, v);
     } else {
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
+        for (int i = 0; i < CW; ++i)
             v[i] = e + i < a.nnz ? to_compute(a.val[e + i]) : typename P::VC(0);
     }
 }
 
 // The tile kernel.  One warp = one worker over tiles [t_begin, t_end).  The stream runs as a
-// software pipeline over the worker's chunks of 8 non-zeros per lane: while chunk g is
+// software pipeline over the worker's chunks of CW non-zeros per lane: while chunk g is
 // multiplied, the values of chunk g+1 and the column indices of chunk g+2 are in flight and the
 // x gathers of chunk g+1 are issued; the bit flags' row_ptr entries and tile_ptr are fetched
 // one tile ahead.
@@ -163,7 +176,8 @@ __global__ void __launch_bounds__(WARPS * 32)
     using XT = typename P::XT;
     using YT = typename P::YT;
     constexpr int TILE = 32 * S;
-    constexpr int NC = S / 8;
+    constexpr int CW = chunk_width<S>();
+    constexpr int NC = S / CW;
     __shared__ uint32_t s_words[WARPS][32];
     __shared__ int s_rowof[WARPS][TILE];
 
@@ -182,17 +196,17 @@ __global__ void __launch_bounds__(WARPS * 32)
     RowBatch rb = prefetch_rows(a.row_ptr, a.m, (int)(tp0 & ROW_MASK));
 
     // pipeline registers: A = chunk g (values, x) and g+1 (columns); B = the next ones
-    int colA[8], colB[8];
-    VC valA[8], valB[8];
-    XT xA[8], xB[8];
+    int colA[CW], colB[CW];
+    VC valA[CW], valB[CW];
+    XT xA[CW], xB[CW];
     {
-        int col0[8];
-        load_cols<P, S>(a, t_begin, 0, lane, pol_s, col0);
-        load_vals<P, S>(a, t_begin, 0, lane, pol_s, valA);
-        gather8(a.x, col0, pol_x, xA);
+        int col0[CW];
+        load_cols<P, S, CW>(a, t_begin, 0, lane, pol_s, col0);
+        load_vals<P, S, CW>(a, t_begin, 0, lane, pol_s, valA);
+        gather_cw(a.x, col0, pol_x, xA);
         const int t1 = t_begin + (NC > 1 ? 0 : 1);
         const int c1 = NC > 1 ? 1 : 0;
-        if (t1 < t_end) load_cols<P, S>(a, t1, c1, lane, pol_s, colA);
+        if (t1 < t_end) load_cols<P, S, CW>(a, t1, c1, lane, pol_s, colA);
     }
 
     int carry_row = -1;  // row of the segment left open by the previous tile (-1: none)
@@ -258,15 +272,15 @@ __global__ void __launch_bounds__(WARPS * 32)
             // issue: columns of chunk g+2, values and x of chunk g+1
             const int t1 = t + (c + 1) / NC, c1 = (c + 1) % NC;
             const int t2 = t + (c + 2) / NC, c2 = (c + 2) % NC;
-            if (t2 < t_end) load_cols<P, S>(a, t2, c2, lane, pol_s, colB);
+            if (t2 < t_end) load_cols<P, S, CW>(a, t2, c2, lane, pol_s, colB);
             if (t1 < t_end) {
-                load_vals<P, S>(a, t1, c1, lane, pol_s, valB);
-                gather8(a.x, colA, pol_x, xB);
+                load_vals<P, S, CW>(a, t1, c1, lane, pol_s, valB);
+                gather_cw(a.x, colA, pol_x, xB);
             }
             // multiply chunk g
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const int kk = c * 8 + k;
+            for (int k = 0; k < CW; ++k) {
+                const int kk = c * CW + k;
                 if ((w >> (31 - kk)) & 1u) {
                     if (cur_row >= 0)
                         store_row(a.y, a.m, cur_row, P::out_acc(run), a.err);  // complete in lane
@@ -278,7 +292,7 @@ __global__ void __launch_bounds__(WARPS * 32)
                 run = P::fma(valA[k], xA[k], run);
             }
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
+            for (int k = 0; k < CW; ++k) {
                 colA[k] = colB[k];
                 valA[k] = valB[k];
                 xA[k] = xB[k];

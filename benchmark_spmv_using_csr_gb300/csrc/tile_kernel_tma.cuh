@@ -81,6 +81,13 @@ __device__ __forceinline__ void smem_cols8(const unsigned char* run, int c, int 
     cc[4] = b.x; cc[5] = b.y; cc[6] = b.z; cc[7] = b.w;
 }
 
+template <typename XT>
+__device__ __forceinline__ void gather8(const XT* __restrict__ x, const int (&c)[8], uint64_t pol,
+                                        XT (&xv)[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) xv[i] = c[i] >= 0 ? ld_x(x + c[i], pol) : XT(0);
+}
+
 template <class P, int S, int WARPS, int NSTAGE>
 __global__ void __launch_bounds__(WARPS * 32, 1)
     k_tiles_tma(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
