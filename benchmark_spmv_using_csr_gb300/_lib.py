@@ -58,6 +58,8 @@ SIGNATURES = {
     "bhsp_bitflags": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "bhsp_validate_csr": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p]),
     "bhsp_version": (c_char_p, []),
+    "bhsp_spmv_f64_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                                      c_int, c_int, c_int, c_void_p]),
     # generators (spmv_gen.h)
     "bhsp_gen_uniform": (c_int, [c_int64, c_uint64, c_double, c_double, c_void_p]),
     "bhsp_gen_uniform_int": (c_int, [c_int64, c_uint64, c_int, c_void_p]),

@@ -30,6 +30,7 @@ BHSPARSE_CUDA_ERROR = -4
 BHSPARSE_NOT_PREPARED = -5
 BHSPARSE_DEVICE_CHECK_FAILED = -6
 BHSPARSE_OUT_OF_MEMORY = -7
+BHSPARSE_NOALLOC_TOO_LARGE = -8
 
 VALUE_F64 = 0
 VALUE_F32 = 1

@@ -29,6 +29,7 @@ extern "C" {
 #define BHSPARSE_NOT_PREPARED -5         /* run/get before prepare_mem */
 #define BHSPARSE_DEVICE_CHECK_FAILED -6  /* a kernel's own bounds check fired */
 #define BHSPARSE_OUT_OF_MEMORY -7
+#define BHSPARSE_NOALLOC_TOO_LARGE -8    /* matrix too large for the fixed scratch of bhsp_spmv_f64_noalloc */
 
 /* Largest nnz accepted (int32 indices with one tile of head-room). */
 #define BHSP_MAX_NNZ 2147479551
@@ -148,6 +149,33 @@ int bhsp_bitflags(const int* d_row_ptr, int m, int nnz, int seg, const uint32_t*
 /* 0 if the CSR is valid, else BHSPARSE_INVALID_CSR (synchronises `stream`). */
 int bhsp_validate_csr(const int* d_row_ptr, const int* d_col_idx, int m, int n, int nnz,
                       void* stream);
+
+/* ------------------------------------------------------------------------------------ */
+/* Allocation-free entry point (no counterpart in the reference).                        */
+/* ------------------------------------------------------------------------------------ */
+/* Size of the fixed device scratch array behind bhsp_spmv_f64_noalloc: 2 MiB, held on every GPU
+ * that loads the library until the process exits.  With the entry point's schedule (16
+ * non-zeros per lane, 8 tiles per worker) it covers matrices of up to about 195 million
+ * non-zeros; larger ones are rejected with BHSPARSE_NOALLOC_TOO_LARGE before any work. */
+#define BHSP_NOALLOC_SCRATCH_BYTES (2u << 20)
+/* y = A.x in plain FP64 for callers that must not allocate device memory: code that runs
+ * inside a host framework which owns all device memory through its own caching allocator,
+ * real-time loops that cannot afford cudaMalloc / cudaFree (both may synchronise the whole
+ * device), or processes whose device footprint must not grow after start-up.  All buffers are
+ * the caller's device pointers (d_val and d_col_idx 32-byte aligned); the kernels' scratch
+ * (tile partition, carry records, error word) lives in the fixed array above, so the call
+ * performs no cudaMalloc, cudaFree or other allocating routine.
+ *   - The first call on each device looks up the array's device address (with that device
+ *     current) and caches it; make that first call before any stream capture.
+ *   - Every call shares the one array: calls whose work overlaps on the GPU (two streams, two
+ *     host threads) race and must not be issued; calls in sequence are safe.
+ *   - The call enqueues on `stream` and synchronises it before returning; it returns
+ *     BHSPARSE_DEVICE_CHECK_FAILED if a kernel's own check fired.
+ *   - validate != 0 first checks the CSR (synchronously) and returns BHSPARSE_INVALID_CSR
+ *     instead of running on invalid input; with validate == 0 the CSR must be valid. */
+int bhsp_spmv_f64_noalloc(const int* d_row_ptr, const int* d_col_idx, const double* d_val,
+                          const double* d_x, double* d_y, int m, int n, int nnz, int validate,
+                          void* stream);
 
 /* Library version string and the compute capability it was built for. */
 const char* bhsp_version(void);
