@@ -74,7 +74,7 @@ __device__ __forceinline__ float to_compute(__nv_bfloat16 v) { return __bfloat16
 // Non-zeros per lane handled per pipeline step (a "chunk"): 4 for S = 8 (two steps per tile,
 // fewer live registers), 8 otherwise.
 template <int S>
-constexpr int chunk_width() {
+__host__ __device__ constexpr int chunk_width() {
     return S == 8 ? 4 : 8;
 }
 
