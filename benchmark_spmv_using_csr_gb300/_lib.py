@@ -58,6 +58,13 @@ SIGNATURES = {
     "bhsp_bitflags": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "bhsp_validate_csr": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p]),
     "bhsp_version": (c_char_p, []),
+    # tuning
+    "bhsp_tune_num_candidates": (c_int, []),
+    "bhsp_tune_candidate": (c_int, [c_int, P_int, P_int, P_int, P_int]),
+    "bhsp_autotune": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                              c_void_p, c_int, c_int, c_void_p, P_int, c_void_p]),
+    "bhsp_row_features": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p]),
+    "bhsp_features_from_counts": (None, [c_int, c_int, c_void_p, c_void_p]),
     "bhsp_spmv_f64_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                                       c_int, c_int, c_int, c_void_p]),
     # generators (spmv_gen.h)

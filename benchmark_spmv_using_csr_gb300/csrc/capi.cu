@@ -221,10 +221,24 @@ static int plan_check(bhsp_plan* p, cudaStream_t st) {
     return BHSPARSE_SUCCESS;
 }
 
+namespace spmv {
+int plan_create_impl(bhsp_plan** out, int value_type, int m, int n, int nnz, const int* d_row_ptr,
+                     const int* d_col_idx, int seg, int tiles_per_worker, int warps_per_cta,
+                     int stages, void* stream, bool validate);
+}
+
 extern "C" int bhsp_plan_create(bhsp_plan** out, int value_type, int m, int n, int nnz,
                                 const int* d_row_ptr, const int* d_col_idx, int seg,
                                 int tiles_per_worker, int warps_per_cta, int stages,
                                 void* stream) {
+    return spmv::plan_create_impl(out, value_type, m, n, nnz, d_row_ptr, d_col_idx, seg,
+                                  tiles_per_worker, warps_per_cta, stages, stream, true);
+}
+
+int spmv::plan_create_impl(bhsp_plan** out, int value_type, int m, int n, int nnz,
+                           const int* d_row_ptr, const int* d_col_idx, int seg,
+                           int tiles_per_worker, int warps_per_cta, int stages, void* stream,
+                           bool validate) {
     if (!out) return BHSPARSE_INVALID_ARGUMENT;
     *out = nullptr;
     if (!valid_vt(value_type) || !supported_vt(value_type)) return BHSPARSE_UNSUPPORTED_VALUE_TYPE;
@@ -236,8 +250,10 @@ extern "C" int bhsp_plan_create(bhsp_plan** out, int value_type, int m, int n, i
     TileConfig cfg = make_config(seg, tiles_per_worker, warps_per_cta, stages);
     if (!config_ok(cfg, value_type)) return BHSPARSE_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    rc = validate_on_device(d_row_ptr, d_col_idx, m, n, nnz, st, &msg);
-    if (rc) return rc;
+    if (validate) {
+        rc = validate_on_device(d_row_ptr, d_col_idx, m, n, nnz, st, &msg);
+        if (rc) return rc;
+    }
     bhsp_plan* p = new bhsp_plan;
     p->vt = value_type;
     p->m = m;

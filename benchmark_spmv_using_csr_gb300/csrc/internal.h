@@ -64,6 +64,15 @@ cudaError_t launch_convert_to_f64(const float* src, double* dst, size_t n, cudaS
 
 inline bool is_supported_value_type(int vt) { return vt >= 0 && vt <= 3; }
 
+}  // namespace spmv
+struct bhsp_plan;
+namespace spmv {
+// bhsp_plan_create with the device-side CSR validation made optional (the autotuner validates
+// once and then builds one plan per candidate schedule).
+int plan_create_impl(bhsp_plan** out, int value_type, int m, int n, int nnz, const int* d_row_ptr,
+                     const int* d_col_idx, int seg, int tiles_per_worker, int warps_per_cta,
+                     int stages, void* stream, bool validate);
+
 // Dynamic shared memory one CTA of the TMA-staged kernel needs (0 for the direct kernel);
 // value_type as in bhsp_value_type.  Configurations above 227 KB cannot run.
 int tile_config_smem_bytes(int value_type, const TileConfig& cfg);

@@ -151,6 +151,30 @@ int bhsp_validate_csr(const int* d_row_ptr, const int* d_col_idx, int m, int n, 
                       void* stream);
 
 /* ------------------------------------------------------------------------------------ */
+/* Schedule tuning (no counterpart in the reference, whose tile geometry is fixed at     */
+/* compile time: spmv_cuda/common.h:39-48).                                              */
+/* ------------------------------------------------------------------------------------ */
+/* The candidate schedules: index -> (non-zeros per lane, tiles per worker, warps per CTA,
+ * stages). */
+int bhsp_tune_num_candidates(void);
+int bhsp_tune_candidate(int index, int* seg, int* tiles_per_worker, int* warps_per_cta,
+                        int* stages);
+/* Autotuner: validates the CSR, then times y = A.x for every candidate on the given device
+ * buffers (`warmup` untimed runs, then the median of `reps` CUDA-event-timed runs) and writes
+ * ms_out[bhsp_tune_num_candidates()] and the index of the fastest to *best.  Synchronous. */
+int bhsp_autotune(int value_type, int m, int n, int nnz, const int* d_row_ptr,
+                  const int* d_col_idx, const void* d_val, const void* d_x, void* d_y, int warmup,
+                  int reps, float* ms_out, int* best, void* stream);
+/* The 16 row-length statistics the learned tuner reads, computed on the device in one pass
+ * over row_ptr:  0 log2(m+1), 1 log2(n+1), 2 log2(nnz+1), 3 log2(1+mean length),
+ * 4 log2(1+std), 5 log2(1+max), 6 empty-row fraction, 7..15 fraction of rows whose length is
+ * 1, 2-3, 4-7, 8-15, 16-31, 32-63, 64-255, 256-4095, >= 4096.  Synchronous. */
+int bhsp_row_features(const int* d_row_ptr, int m, int n, float* features16, void* stream);
+/* The same features from the 13 accumulated counts (sum, sum of squares, max, empty rows,
+ * 9 bin counts); host arithmetic shared by the device path and CPU checks. */
+void bhsp_features_from_counts(int m, int n, const unsigned long long* counts13, float* features16);
+
+/* ------------------------------------------------------------------------------------ */
 /* Allocation-free entry point (no counterpart in the reference).                        */
 /* ------------------------------------------------------------------------------------ */
 /* Size of the fixed device scratch array behind bhsp_spmv_f64_noalloc: 2 MiB, held on every GPU
