@@ -58,6 +58,14 @@ SIGNATURES = {
     "bhsp_bitflags": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "bhsp_validate_csr": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p]),
     "bhsp_version": (c_char_p, []),
+    # batched form
+    "bhsp_batch_create": (c_int, [P_void, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int,
+                                  c_int, c_int, c_int, c_void_p]),
+    "bhsp_batch_execute": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "bhsp_batch_check": (c_int, [c_void_p, c_void_p]),
+    "bhsp_batch_info": (c_int, [c_void_p, P_int, P_int, P_int, P_int]),
+    "bhsp_batch_last_error": (c_char_p, [c_void_p]),
+    "bhsp_batch_destroy": (None, [c_void_p]),
     # tuning
     "bhsp_tune_num_candidates": (c_int, []),
     "bhsp_tune_candidate": (c_int, [c_int, P_int, P_int, P_int, P_int]),

@@ -25,6 +25,10 @@ __device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
     return make_float2(s, __fadd_rn(__fadd_rn(a.y, b.y), es));
 }
 
+// The carry of a worker's open row stays a float-float pair (compensated, about 48 significant
+// bits) from tile to tile -- converting to FP64 on every tile would cost two conversions and
+// two adds on GB300's narrow FP64 pipe per tile -- and becomes FP64 when the row is handed to
+// another worker (the carry record) and in the calibration that adds those records.
 template <typename VSTORE>
 struct PolMixed {
     using VS = VSTORE;
@@ -32,16 +36,20 @@ struct PolMixed {
     using XT = float;
     using YT = float;
     using Acc = float2;
-    using Carry = double;
+    using Carry = float2;
+    using Rec = double;
     __device__ static float2 zero() { return make_float2(0.f, 0.f); }
-    __device__ static double carry_zero() { return 0.0; }
+    __device__ static float2 carry_zero() { return make_float2(0.f, 0.f); }
     __device__ static float2 fma(float v, float x, float2 a) { return ff_add_product(v, x, a); }
     __device__ static float2 add(float2 a, float2 b) { return ff_add(a, b); }
-    __device__ static double carry_from(float2 a) { return (double)a.x + (double)a.y; }
-    __device__ static double carry_add(double c, float2 a) { return c + ((double)a.x + (double)a.y); }
+    __device__ static float2 carry_from(float2 a) { return a; }
+    __device__ static float2 carry_add(float2 c, float2 a) { return ff_add(c, a); }
     __device__ static float out_acc(float2 a) { return __fadd_rn(a.x, a.y); }
-    __device__ static float out_carry(double c) { return __double2float_rn(c); }
-    __device__ static double carry_of_y(float y) { return (double)y; }
+    __device__ static float out_carry(float2 c) { return __fadd_rn(c.x, c.y); }
+    __device__ static double rec_from(float2 c) { return (double)c.x + (double)c.y; }
+    __device__ static double rec_add(double a, double b) { return a + b; }
+    __device__ static double rec_of_y(float y) { return (double)y; }
+    __device__ static float out_rec(double r) { return __double2float_rn(r); }
 };
 
 cudaError_t launch_mixed(const MixedLaunch& l, const TileConfig& cfg, cudaStream_t st) {

@@ -21,7 +21,11 @@ struct PolF64 {
     __device__ static double carry_from(double a) { return a; }
     __device__ static double out_acc(double a) { return a; }
     __device__ static double out_carry(double c) { return c; }
-    __device__ static double carry_of_y(double y) { return y; }
+    using Rec = double;
+    __device__ static double rec_from(double c) { return c; }
+    __device__ static double rec_add(double a, double b) { return a + b; }
+    __device__ static double rec_of_y(double y) { return y; }
+    __device__ static double out_rec(double r) { return r; }
 };
 
 struct PolF32 {
@@ -39,7 +43,11 @@ struct PolF32 {
     __device__ static float carry_from(float a) { return a; }
     __device__ static float out_acc(float a) { return a; }
     __device__ static float out_carry(float c) { return c; }
-    __device__ static float carry_of_y(float y) { return y; }
+    using Rec = float;
+    __device__ static float rec_from(float c) { return c; }
+    __device__ static float rec_add(float a, float b) { return a + b; }
+    __device__ static float rec_of_y(float y) { return y; }
+    __device__ static float out_rec(float r) { return r; }
 };
 
 template <class P>
@@ -52,7 +60,7 @@ static cudaError_t launch_plain_any(const PlainLaunch& l, const TileConfig& cfg,
     a.y = static_cast<typename P::YT*>(l.y);
     a.tile_ptr = l.tile_ptr;
     a.rec_row = l.rec_row;
-    a.rec_val = static_cast<typename P::Carry*>(l.rec_val);
+    a.rec_val = static_cast<typename P::Rec*>(l.rec_val);
     a.err = l.err;
     a.m = l.m;
     a.n = l.n;

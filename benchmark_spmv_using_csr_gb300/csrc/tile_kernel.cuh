@@ -28,8 +28,13 @@
 //    repeated calls give the same y.
 //
 // The arithmetic policy P fixes the storage types and the accumulate / carry arithmetic:
-// plain FP64 and FP32 (Acc = Carry = value type, one FMA per non-zero) and the mixed forms
-// (FP32 or BF16 values, FP32 x and y, compensated float-float Acc, FP64 Carry).
+// plain FP64 and FP32 (accumulator, carry and record all in the value type, one FMA per
+// non-zero) and the mixed forms (FP32 or BF16 values, FP32 x and y, compensated float-float
+// accumulator and within-worker carry, FP64 carry records and calibration).
+//
+// Policy interface: Acc (per-lane accumulator): zero, fma, add; Carry (a worker's open row):
+// carry_zero, carry_add(Carry, Acc), carry_from(Acc), out_carry -> YT; Rec (a carry record
+// between workers): rec_from(Carry), rec_add, rec_of_y(YT), out_rec -> YT; out_acc(Acc) -> YT.
 #pragma once
 #include "tile.cuh"
 
@@ -44,7 +49,7 @@ struct TileArgs {
     typename P::YT* __restrict__ y;
     const uint32_t* __restrict__ tile_ptr;
     int* __restrict__ rec_row;
-    typename P::Carry* __restrict__ rec_val;
+    typename P::Rec* __restrict__ rec_val;
     uint32_t* err;
     int m, n, nnz;
     int phase;  // bit 0: tile kernel, bit 1: calibration kernel
@@ -73,9 +78,10 @@ __device__ __forceinline__ float to_compute(__nv_bfloat16 v) { return __bfloat16
 
 // Non-zeros per lane handled per pipeline step (a "chunk"): 4 for S = 8 (two steps per tile,
 // fewer live registers), 8 otherwise.
-template <int S>
+template <int S, typename XT>
 __host__ __device__ constexpr int chunk_width() {
-    return S == 8 ? 4 : 8;
+    // x entries wider than 8 bytes (several right-hand sides) use 4-wide chunks too
+    return (S == 8 || sizeof(XT) > 8) ? 4 : 8;
 }
 
 template <int CW, typename XT>
@@ -167,29 +173,22 @@ __device__ __forceinline__ void load_vals(const TileArgs<P>& a, int t, int c, in
 // multiplied, the values of chunk g+1 and the column indices of chunk g+2 are in flight and the
 // x gathers of chunk g+1 are issued; the bit flags' row_ptr entries and tile_ptr are fetched
 // one tile ahead.
-template <class P, int S, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
-    k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
+template <class P, int S>
+__device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, int tpw, int ntiles,
+                                            uint32_t* const s_words_w, int* const rowof) {
     using Acc = typename P::Acc;
     using Carry = typename P::Carry;
     using VC = typename P::VC;
     using XT = typename P::XT;
     using YT = typename P::YT;
     constexpr int TILE = 32 * S;
-    constexpr int CW = chunk_width<S>();
+    constexpr int CW = chunk_width<S, typename P::XT>();
     constexpr int NC = S / CW;
-    __shared__ uint32_t s_words[WARPS][32];
-    __shared__ int s_rowof[WARPS][TILE];
-
-    const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int worker = blockIdx.x * WARPS + warp;
-    if (worker >= nworkers) return;
     const int t_begin = worker * tpw;
     const int t_end = min(t_begin + tpw, ntiles);
     const uint64_t pol_s = policy_evict_first();
     const uint64_t pol_x = policy_evict_last();
-    int* const rowof = s_rowof[warp];
 
     uint32_t tp0 = __ldg(a.tile_ptr + t_begin);
     uint32_t tp1 = __ldg(a.tile_ptr + t_begin + 1);
@@ -221,7 +220,7 @@ __global__ void __launch_bounds__(WARPS * 32)
                 store_row(a.y, a.m, row, P::out_carry(v), a.err);
             } else {
                 a.rec_row[worker] = row;
-                a.rec_val[worker] = v;
+                a.rec_val[worker] = P::rec_from(v);
             }
         }
         if (!owned) rec_written = true;
@@ -236,7 +235,7 @@ __global__ void __launch_bounds__(WARPS * 32)
             tp2 = __ldg(a.tile_ptr + t + 2);
             rbn = prefetch_rows(a.row_ptr, a.m, hi);
         }
-        const uint32_t w = tile_rows<S, YT>(a.row_ptr, a.m, t * TILE, lo, hi, rb, s_words[warp],
+        const uint32_t w = tile_rows<S, YT>(a.row_ptr, a.m, t * TILE, lo, hi, rb, s_words_w,
                                             rowof, a.y);
         const bool first_head = ((__shfl_sync(SPMV_FULL_MASK, w, 0) >> 31) & 1u) != 0u;
         const uint32_t fmask = __ballot_sync(SPMV_FULL_MASK, w != 0u);
@@ -357,28 +356,64 @@ __global__ void __launch_bounds__(WARPS * 32)
     if (!rec_written && lane == 0) a.rec_row[worker] = -1;
 }
 
+// One warp = one worker, worker = global warp index (static schedule).
+template <class P, int S, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
+    __shared__ uint32_t s_words[WARPS][32];
+    __shared__ int s_rowof[WARPS][32 * S];
+    const int warp = threadIdx.x >> 5;
+    const int worker = blockIdx.x * WARPS + warp;
+    if (worker >= nworkers) return;
+    tile_worker<P, S>(a, worker, tpw, ntiles, s_words[warp], s_rowof[warp]);
+}
+
+// Persistent schedule: a grid sized to the GPU's resident capacity; each warp takes the next
+// worker index from a global ticket until none is left (the global tile work queue of the
+// batched form: workers are consecutive tile ranges, so the ticket walks the tiles in order).
+template <class P, int S, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_tiles_persistent(TileArgs<P> a, int tpw, int nworkers, int ntiles, int* ticket) {
+    __shared__ uint32_t s_words[WARPS][32];
+    __shared__ int s_rowof[WARPS][32 * S];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int w = 0;
+        if (lane == 0) w = atomicAdd(ticket, 1);
+        w = __shfl_sync(SPMV_FULL_MASK, w, 0);
+        if (w >= nworkers) break;
+        if (w < 0) {  // cannot happen with a ticket reset to 0 before the launch
+            if (lane == 0) atomicOr(a.err, ERR_QUEUE);
+            break;
+        }
+        tile_worker<P, S>(a, w, tpw, ntiles, s_words[warp], s_rowof[warp]);
+        __syncwarp();
+    }
+}
+
 // Carry records -> y, in worker order (deterministic): the first record of each run of equal
 // rows sums the run and adds it to the owner's value.  Also zeroes the leading empty rows,
 // which lie in no tile span (the reference never writes them).
 template <class P>
 __global__ void k_calibrate(const int* __restrict__ rec_row,
-                            const typename P::Carry* __restrict__ rec_val, int nworkers,
+                            const typename P::Rec* __restrict__ rec_val, int nworkers,
                             typename P::YT* __restrict__ y, const uint32_t* __restrict__ tile_ptr,
                             int m, uint32_t* err) {
-    using Carry = typename P::Carry;
+    using Rec = typename P::Rec;
     const int stride = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     for (int w = tid; w < nworkers; w += stride) {
         const int r = rec_row[w];
         if (r < 0) continue;
         if (w > 0 && rec_row[w - 1] == r) continue;
-        Carry s = rec_val[w];
-        for (int v = w + 1; v < nworkers && rec_row[v] == r; ++v) s = s + rec_val[v];
+        Rec s = rec_val[w];
+        for (int v = w + 1; v < nworkers && rec_row[v] == r; ++v) s = P::rec_add(s, rec_val[v]);
         if (r >= m) {
             atomicOr(err, ERR_BAD_TILE);
             continue;
         }
-        y[r] = P::out_carry(P::carry_of_y(y[r]) + s);
+        y[r] = P::out_rec(P::rec_add(P::rec_of_y(y[r]), s));
     }
     const int lead = min((int)(tile_ptr[0] & ROW_MASK), m);
     for (int r = tid; r < lead; r += stride) y[r] = typename P::YT(0);

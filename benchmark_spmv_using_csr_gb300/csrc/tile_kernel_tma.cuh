@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
                 store_row(a.y, a.m, row, P::out_carry(v), a.err);
             } else {
                 a.rec_row[worker] = row;
-                a.rec_val[worker] = v;
+                a.rec_val[worker] = P::rec_from(v);
             }
         }
         if (!owned) rec_written = true;

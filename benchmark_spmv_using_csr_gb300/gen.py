@@ -165,3 +165,41 @@ def stencil27_160(seed: int = 3) -> CSR:
 
 WORKLOADS = {"stencil5_256": stencil5_256, "powerlaw_4m": powerlaw_4m,
              "stencil27_160": stencil27_160}
+
+
+# --- the batched workload: many matrices of uneven size from a mix of generators -----------
+BATCH_KINDS = ("stencil2d", "stencil3d", "powerlaw", "density", "blockdiag")
+
+
+def batch_member(m_target: int, kind: str, seed: int) -> CSR:
+    """One square matrix of about m_target rows from the named generator."""
+    if kind == "stencil2d":
+        nx = max(1, int(round(m_target ** 0.5)))
+        return stencil2d(nx, max(1, int(round(m_target / nx))), seed=seed)
+    if kind == "stencil3d":
+        nx = max(1, int(round(m_target ** (1.0 / 3.0))))
+        ny = nx
+        return stencil3d(nx, ny, max(1, int(round(m_target / (nx * ny)))), seed=seed)
+    if kind == "powerlaw":
+        return powerlaw(m_target, seed=seed)
+    if kind == "density":
+        return density(m_target, m_target, 1e-4, seed=seed)
+    if kind == "blockdiag":
+        return blockdiag(m_target, m_target, 32, seed=seed)
+    raise ValueError(kind)
+
+
+def batch_workload(count: int = 512, m_lo: int = 1_000, m_hi: int = 200_000, seed: int = 4,
+                   kinds=BATCH_KINDS) -> list:
+    """`count` matrices with row counts log-uniform in [m_lo, m_hi], each drawn from a seeded
+    mix of generators (2D/3D stencil, power-law rows, uniform density 1e-4, block-diagonal
+    32x32 dense blocks)."""
+    u = uniform(2 * count, seed, 0.0, 1.0)
+    mats = []
+    for i in range(count):
+        m = int(round(np.exp(np.log(m_lo) + u[2 * i] * (np.log(m_hi) - np.log(m_lo)))))
+        kind = kinds[min(int(u[2 * i + 1] * len(kinds)), len(kinds) - 1)]
+        a = batch_member(m, kind, seed * 100_003 + i)
+        a.name = f"{kind}_{a.m}"
+        mats.append(a)
+    return mats

@@ -151,6 +151,33 @@ int bhsp_validate_csr(const int* d_row_ptr, const int* d_col_idx, int m, int n, 
                       void* stream);
 
 /* ------------------------------------------------------------------------------------ */
+/* Batched multi-RHS form (no counterpart in the reference).                             */
+/* ------------------------------------------------------------------------------------ */
+/* Many CSR matrices and k in {1,2,4,8} right-hand sides per launch, FP32 storage, compensated
+ * FP32 accumulation (the mixed form's arithmetic), FP64 carry records.  The batch is passed as
+ * one block-diagonal CSR (device pointers, kept by the caller):
+ *   d_row_ptr[m_total+1]: the matrices' row pointers concatenated, with global non-zero offsets;
+ *   d_col_idx[nnz_total]: each matrix's column indices plus the offset of its x block
+ *                         (32-byte aligned).
+ * x is [n_total][k] and y is [m_total][k], the k values of a row interleaved.  One persistent
+ * kernel hands out tile ranges from a global ticket; schedule fields as in bhsp_set_config
+ * (0 = default).  Validates the CSR and builds the partition (synchronous). */
+typedef struct bhsp_batch bhsp_batch;
+int bhsp_batch_create(bhsp_batch** out, int count, int m_total, int n_total, int nnz_total,
+                      const int* d_row_ptr, const int* d_col_idx, int k, int seg,
+                      int tiles_per_worker, int warps_per_cta, void* stream);
+/* y = A.x for all matrices and right-hand sides, enqueued on `stream`.  use_graph != 0 replays a
+ * CUDA graph of the ticket reset, the persistent kernel and the calibration (captured on the
+ * first call and again whenever the buffers change); use_graph == 0 launches them directly.
+ * d_val 32-byte aligned, d_x / d_y aligned to 4*k bytes. */
+int bhsp_batch_execute(bhsp_batch* b, const float* d_val, const float* d_x, float* d_y,
+                       int use_graph, void* stream);
+int bhsp_batch_check(bhsp_batch* b, void* stream);
+int bhsp_batch_info(const bhsp_batch* b, int* ntiles, int* nworkers, int* grid, int* launches);
+const char* bhsp_batch_last_error(const bhsp_batch* b);
+void bhsp_batch_destroy(bhsp_batch* b);
+
+/* ------------------------------------------------------------------------------------ */
 /* Schedule tuning (no counterpart in the reference, whose tile geometry is fixed at     */
 /* compile time: spmv_cuda/common.h:39-48).                                              */
 /* ------------------------------------------------------------------------------------ */
