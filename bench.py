@@ -229,9 +229,12 @@ def run_ours(args) -> None:
     x_pin = torch.from_numpy(x).pin_memory()
     y_pin = torch.zeros(a.m, dtype=torch.float64).pin_memory()
     y_np = y_pin.numpy()
+    tuning = None
+    if args.config is None:  # the autotuner picks the schedule on this matrix
+        tuning = autotune_workload(a, x)
+        args.config = tuning["pick"]
     h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
-    if args.config is not None:
-        assert h.set_config(*args.config) == 0, h.last_error
+    assert h.set_config(*args.config) == 0, h.last_error
     seg, tpw, warps, stages = h.get_config()
     assert h.set_device(local) == 0
     assert h.init_platform() == 0, h.last_error
@@ -344,6 +347,7 @@ def run_ours(args) -> None:
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT,
                     "h2d_bytes_per_step": a.n * 8, "d2h_bytes_per_step": a.m * 8,
                     "path": "bhsp_set_x + bhsp_run_benchmark + bhsp_get_y, pinned host x/y"},
+            "tuning": tuning,
             "gpu_launches": 2 * args.steps,
             "clocks": clocks,
             "prepare_mem_s": round(t_prep, 3),
@@ -353,6 +357,8 @@ def run_ours(args) -> None:
 
     if rank == 0 and args.forms:
         line["forms"] = measure_forms(args, a, x, ystar)
+    if rank == 0 and args.batched:
+        line["batched"] = measure_batched(args)
     if rank == 0 and args.cpu_baseline > 0:
         line["cpu_baseline"] = cpu_baseline(a, x, B, args.cpu_baseline)
     if rank == 0:
@@ -404,6 +410,100 @@ def measure_forms(args, a, x, ystar) -> dict:
     return out
 
 
+def autotune_workload(a, x) -> dict:
+    """Run the library's autotuner (every candidate schedule, median of 5 timed runs) on the
+    workload and return its table and pick."""
+    import torch
+
+    import benchmark_spmv_using_csr_gb300 as sp
+    from benchmark_spmv_using_csr_gb300 import tune
+    rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
+    val, xd = torch.from_numpy(a.val).cuda(), torch.from_numpy(x).cuda()
+    y = torch.zeros(a.m, dtype=torch.float64, device="cuda")
+    ms, best = tune.autotune(sp.VALUE_F64, rp, ci, val, xd, y, warmup=2, reps=5)
+    cands = tune.candidates()
+    del rp, ci, val, xd, y
+    torch.cuda.empty_cache()
+    return {"pick": list(cands[best]), "best_ms": float(ms[best]),
+            "table_ms": {",".join(map(str, c)): round(float(t), 4) for c, t in zip(cands, ms)}}
+
+
+def measure_batched(args) -> dict:
+    """The batched workload: 512 matrices (rows log-uniform in [1e3, 2e5], mixed generators),
+    FP32 storage with compensated accumulation, k right-hand sides, one persistent kernel
+    replayed from a CUDA graph -- against the plain FP64 form launched once per matrix and
+    right-hand side (512*k sequential plain launches).  nnz*k per second, and the normwise
+    error of a subset of matrices against the FP64 oracle."""
+    import numpy as np
+    import torch
+
+    import benchmark_spmv_using_csr_gb300 as sp
+    import oracle
+    from benchmark_spmv_using_csr_gb300 import batch, gen
+    mats = gen.batch_workload(512)
+    nnz = sum(a.nnz for a in mats)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        evs = []
+        for i in range(reps):
+            flush.fill_(i & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        return statistics.median(p.elapsed_time(q) for p, q in evs)
+
+    plans = []
+    for a in mats:
+        rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
+        v = torch.from_numpy(a.val).cuda()
+        xx = torch.from_numpy(gen.uniform(a.n, 1)).cuda()
+        yy = torch.zeros(a.m, dtype=torch.float64, device="cuda")
+        plans.append((sp.Plan(sp.VALUE_F64, a.m, a.n, rp, ci), rp, ci, v, xx, yy))
+
+    def plain_all():
+        for p, _, _, v, xx, yy in plans:
+            p.execute(v, xx, yy)
+    ms_plain = timed(plain_all, 5)
+    out = {"matrices": len(mats), "nnz": nnz, "rows": sum(a.m for a in mats),
+           "plain_fp64_sequential": {"ms_per_rhs": round(ms_plain, 4),
+                                     "gnnz_per_s": round(nnz / ms_plain / 1e6, 2),
+                                     "launches_per_rhs": 2 * len(mats)}}
+    for p in plans:
+        p[0].close()
+    del plans
+    torch.cuda.empty_cache()
+    for k in (1, 2, 4, 8):
+        b = batch.Batch(mats, k=k)
+        xh = gen.uniform(b.n * k, 3).reshape(b.n, k).astype(np.float32)
+        xd = torch.from_numpy(xh).cuda()
+        yd = torch.zeros((b.m, k), dtype=torch.float32, device="cuda")
+        ms = timed(lambda: b.execute(xd, yd, use_graph=True), 10)
+        b.check()
+        ys, no = b.split(yd.cpu().numpy()), b.cat["n_off"]
+        worst = 0.0
+        for i in range(0, len(mats), 23):
+            a = mats[i]
+            for j in range(k):
+                ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, xh[no[i]:no[i + 1], j].astype(np.float64))
+                if np.linalg.norm(ystar) > 0:
+                    worst = max(worst, oracle.normwise_error(ys[i][:, j], ystar))
+        gk = nnz * k / ms / 1e6
+        out[f"k{k}"] = {"ms": round(ms, 4), "gnnz_k_per_s": round(gk, 2),
+                        "vs_plain_fp64_sequential": round(ms_plain * k / ms, 2),
+                        "normwise_err_vs_fp64_oracle_max": worst, "launches": b.info()["launches"],
+                        "graph": True}
+        b.close()
+        del xd, yd
+        torch.cuda.empty_cache()
+    return out
+
+
 def cpu_baseline(a, x, B, seconds: float) -> dict:
     """The reference's serial CSR loop (spmv_cuda/main.cu:755-761, C port) on one host core,
     whole-matrix passes until `seconds` have elapsed."""
@@ -432,11 +532,13 @@ def main() -> None:
     ap.add_argument("--workload", choices=tuple(WORKLOAD_TEXT), default="powerlaw_4m")
     ap.add_argument("--config", type=int, nargs=4, default=None,
                     metavar=("NNZ_PER_LANE", "TILES_PER_WORKER", "WARPS_PER_CTA", "STAGES"),
-                    help="tile schedule (default: the library's default)")
+                    help="tile schedule (default: the autotuner's pick on this matrix)")
     ap.add_argument("--soak", type=float, default=1.5, help="seconds of untimed steps for clocks")
     ap.add_argument("--cpu-baseline", type=float, default=10.0,
                     help="seconds of serial CPU baseline (0 = skip)")
     ap.add_argument("--no-forms", dest="forms", action="store_false")
+    ap.add_argument("--no-batched", dest="batched", action="store_false",
+                    help="skip the batched multi-RHS measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -66,6 +66,18 @@ SIGNATURES = {
     "bhsp_batch_info": (c_int, [c_void_p, P_int, P_int, P_int, P_int]),
     "bhsp_batch_last_error": (c_char_p, [c_void_p]),
     "bhsp_batch_destroy": (None, [c_void_p]),
+    # learned tuner network
+    "bhsp_mlp_create": (c_int, [P_void, c_int, c_int, c_int, c_int]),
+    "bhsp_mlp_num_params": (c_size_t, [c_void_p]),
+    "bhsp_mlp_set_params": (c_int, [c_void_p, c_void_p, c_size_t]),
+    "bhsp_mlp_get_params": (c_int, [c_void_p, c_void_p, c_size_t]),
+    "bhsp_mlp_set_normalization": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "bhsp_mlp_forward": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
+    "bhsp_mlp_gradients": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
+                                   c_void_p]),
+    "bhsp_mlp_train_step": (c_int, [c_void_p, c_void_p, c_void_p, c_int, ctypes.c_float,
+                                    ctypes.c_float, c_void_p, c_void_p]),
+    "bhsp_mlp_destroy": (None, [c_void_p]),
     # tuning
     "bhsp_tune_num_candidates": (c_int, []),
     "bhsp_tune_candidate": (c_int, [c_int, P_int, P_int, P_int, P_int]),

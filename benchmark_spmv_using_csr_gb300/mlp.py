@@ -1,0 +1,221 @@
+"""The learned schedule tuner: a small MLP (16 row-length features -> 64 -> 64 -> one logit per
+candidate schedule) trained on the autotuner's own timing tables by the library's CUDA kernels
+(bhsp_mlp_*), with the full autotune sweep as its fallback below a confidence threshold.
+
+It only chooses a schedule: whichever schedule it picks, y = A.x is computed by the same
+kernels and arithmetic.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import tune
+from ._lib import lib
+
+HIDDEN = 64
+
+
+def soft_targets(ms: np.ndarray, temperature: float = 0.05) -> np.ndarray:
+    """Training targets from a timing table: probability mass on every schedule within a few
+    per cent of the best, p_k ~ exp(-(ms_k / ms_best - 1) / temperature)."""
+    ms = np.asarray(ms, np.float64)
+    rel = ms / ms.min(axis=-1, keepdims=True) - 1.0
+    w = np.exp(-rel / temperature)
+    return (w / w.sum(axis=-1, keepdims=True)).astype(np.float32)
+
+
+def init_params(n_in: int, hidden: int, n_out: int, seed: int = 0) -> np.ndarray:
+    """He-normal weights, zero biases, in the network's flat layout."""
+    rng = np.random.default_rng(seed)
+    W1 = rng.standard_normal((hidden, n_in)) * np.sqrt(2.0 / n_in)
+    W2 = rng.standard_normal((hidden, hidden)) * np.sqrt(2.0 / hidden)
+    W3 = rng.standard_normal((n_out, hidden)) * np.sqrt(1.0 / hidden)
+    return np.concatenate([W1.ravel(), np.zeros(hidden), W2.ravel(), np.zeros(hidden),
+                           W3.ravel(), np.zeros(n_out)]).astype(np.float32)
+
+
+class MLP:
+    """Device network (bhsp_mlp) with host-side parameter and normalisation access."""
+
+    def __init__(self, n_in: int = tune.NUM_FEATURES, hidden: int = HIDDEN, n_out: int = 18,
+                 max_batch: int = 4096, seed: int = 0):
+        self.n_in, self.hidden, self.n_out, self.max_batch = n_in, hidden, n_out, max_batch
+        self._m = ctypes.c_void_p()
+        rc = lib().bhsp_mlp_create(ctypes.byref(self._m), n_in, hidden, n_out, max_batch)
+        if rc != 0:
+            raise RuntimeError(f"bhsp_mlp_create failed ({rc})")
+        self.mean = np.zeros(n_in, np.float32)
+        self.std = np.ones(n_in, np.float32)
+        self.set_params(init_params(n_in, hidden, n_out, seed))
+
+    @property
+    def num_params(self) -> int:
+        return int(lib().bhsp_mlp_num_params(self._m))
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        if lib().bhsp_mlp_set_params(self._m, p.ctypes.data_as(ctypes.c_void_p), p.size) != 0:
+            raise RuntimeError("bhsp_mlp_set_params failed")
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.num_params, np.float32)
+        if lib().bhsp_mlp_get_params(self._m, p.ctypes.data_as(ctypes.c_void_p), p.size) != 0:
+            raise RuntimeError("bhsp_mlp_get_params failed")
+        return p
+
+    def set_normalization(self, mean, std) -> None:
+        self.mean = np.ascontiguousarray(mean, np.float32)
+        self.std = np.ascontiguousarray(np.maximum(std, 1e-6), np.float32)
+        rc = lib().bhsp_mlp_set_normalization(self._m, self.mean.ctypes.data_as(ctypes.c_void_p),
+                                              self.std.ctypes.data_as(ctypes.c_void_p))
+        if rc != 0:
+            raise RuntimeError("bhsp_mlp_set_normalization failed")
+
+    def _dev(self, a):
+        import torch
+        return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+    def forward(self, feats: np.ndarray) -> np.ndarray:
+        import torch
+        f = self._dev(np.atleast_2d(feats))
+        out = np.zeros((f.shape[0], self.n_out), np.float32)
+        for s in range(0, f.shape[0], self.max_batch):
+            fb = f[s:s + self.max_batch]
+            p = torch.empty((fb.shape[0], self.n_out), dtype=torch.float32, device="cuda")
+            rc = lib().bhsp_mlp_forward(self._m, fb.data_ptr(), fb.shape[0], p.data_ptr(),
+                                        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+            if rc != 0:
+                raise RuntimeError("bhsp_mlp_forward failed")
+            out[s:s + fb.shape[0]] = p.cpu().numpy()
+        return out
+
+    def gradients(self, feats: np.ndarray, targets: np.ndarray) -> tuple[np.ndarray, float]:
+        import torch
+        f, t = self._dev(feats), self._dev(targets)
+        g = torch.empty(self.num_params, dtype=torch.float32, device="cuda")
+        loss = ctypes.c_float()
+        rc = lib().bhsp_mlp_gradients(self._m, f.data_ptr(), t.data_ptr(), f.shape[0], g.data_ptr(),
+                                      ctypes.byref(loss),
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if rc != 0:
+            raise RuntimeError("bhsp_mlp_gradients failed")
+        return g.cpu().numpy(), float(loss.value)
+
+    def train_step(self, f_dev, t_dev, lr: float, weight_decay: float = 0.0) -> float:
+        import torch
+        loss = ctypes.c_float()
+        rc = lib().bhsp_mlp_train_step(self._m, f_dev.data_ptr(), t_dev.data_ptr(), f_dev.shape[0],
+                                       ctypes.c_float(lr), ctypes.c_float(weight_decay),
+                                       ctypes.byref(loss),
+                                       ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if rc != 0:
+            raise RuntimeError("bhsp_mlp_train_step failed")
+        return float(loss.value)
+
+    def close(self) -> None:
+        if self._m:
+            lib().bhsp_mlp_destroy(self._m)
+            self._m = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LearnedTuner:
+    """Features -> schedule, trained on autotuner timing tables; falls back to the sweep."""
+
+    def __init__(self, n_out: int | None = None, hidden: int = HIDDEN, seed: int = 0):
+        self.n_out = len(tune.candidates()) if n_out is None else n_out
+        self.net = MLP(tune.NUM_FEATURES, hidden, self.n_out, seed=seed)
+        self.threshold = 0.0
+
+    def fit(self, feats: np.ndarray, ms: np.ndarray, epochs: int = 400, batch: int = 256,
+            lr: float = 3e-3, weight_decay: float = 1e-4, temperature: float = 0.05,
+            seed: int = 0) -> list:
+        """Train on (features, timing table) pairs with the device kernels; returns the
+        per-epoch mean loss."""
+        import torch
+        feats = np.asarray(feats, np.float32)
+        mean, std = feats.mean(0), feats.std(0)
+        std[std < 1e-6] = 1.0
+        self.net.set_normalization(mean, std)
+        targets = soft_targets(ms, temperature)
+        f_dev, t_dev = self.net._dev(feats), self.net._dev(targets)
+        rng = np.random.default_rng(seed)
+        hist = []
+        n = feats.shape[0]
+        for ep in range(epochs):
+            perm = torch.from_numpy(rng.permutation(n)).cuda()
+            step_lr = lr * 0.5 * (1 + np.cos(np.pi * ep / epochs))  # cosine decay
+            losses = []
+            for s in range(0, n, batch):
+                idx = perm[s:s + batch]
+                losses.append(self.net.train_step(f_dev[idx].contiguous(), t_dev[idx].contiguous(),
+                                                  step_lr, weight_decay))
+            hist.append(float(np.mean(losses)))
+        return hist
+
+    def predict(self, feats: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """(picked candidate index, confidence = its probability) per row of features."""
+        p = self.net.forward(np.atleast_2d(feats))
+        return p.argmax(1), p.max(1)
+
+    def calibrate_threshold(self, feats, ms, target: float = 0.95, max_fallback: float = 0.2) -> float:
+        """Smallest confidence threshold whose non-fallback picks reach `target` of the best
+        time on average (searched on held-in data), capped so at most `max_fallback` of the
+        matrices fall back."""
+        pick, conf = self.predict(feats)
+        frac = ms.min(1) / ms[np.arange(len(pick)), pick]
+        order = np.sort(np.unique(conf))
+        self.threshold = 0.0
+        for th in np.concatenate([[0.0], order]):
+            keep = conf >= th
+            if (~keep).mean() > max_fallback:
+                break
+            mixed = np.where(keep, frac, 1.0)
+            self.threshold = float(th)
+            if mixed.mean() >= target:
+                break
+        return self.threshold
+
+    def evaluate(self, feats, ms) -> dict:
+        """Fraction of the autotuner's best time per matrix (best_ms / picked_ms), with the
+        sweep standing in below the confidence threshold."""
+        pick, conf = self.predict(feats)
+        fb = conf < self.threshold
+        frac = ms.min(1) / ms[np.arange(len(pick)), pick]
+        frac_with_fb = np.where(fb, 1.0, frac)
+        return {"mean_frac_of_best": float(frac_with_fb.mean()),
+                "min_frac_of_best": float(frac_with_fb.min()),
+                "mean_frac_without_fallback": float(frac.mean()),
+                "fallback_rate": float(fb.mean()), "threshold": self.threshold}
+
+    def choose(self, value_type: int, row_ptr, col_idx, val, x, y, n: int | None = None) -> dict:
+        """Pick a schedule for a device matrix: the network if confident, else the sweep."""
+        n = x.numel() if n is None else n
+        f = tune.row_features(row_ptr, n)
+        pick, conf = self.predict(f)
+        if conf[0] >= self.threshold:
+            return {"index": int(pick[0]), "confidence": float(conf[0]), "fallback": False,
+                    "config": tune.candidates()[int(pick[0])]}
+        ms, best = tune.autotune(value_type, row_ptr, col_idx, val, x, y, n=n)
+        return {"index": best, "confidence": float(conf[0]), "fallback": True,
+                "config": tune.candidates()[best], "ms": ms}
+
+    def save(self, path: str) -> None:
+        np.savez(path, params=self.net.get_params(), mean=self.net.mean, std=self.net.std,
+                 threshold=np.float32(self.threshold), n_out=self.n_out, hidden=self.net.hidden)
+
+    @classmethod
+    def load(cls, path: str) -> "LearnedTuner":
+        d = np.load(path)
+        t = cls(n_out=int(d["n_out"]), hidden=int(d["hidden"]))
+        t.net.set_params(d["params"])
+        t.net.set_normalization(d["mean"], d["std"])
+        t.threshold = float(d["threshold"])
+        return t

@@ -202,6 +202,31 @@ int bhsp_row_features(const int* d_row_ptr, int m, int n, float* features16, voi
 void bhsp_features_from_counts(int m, int n, const unsigned long long* counts13, float* features16);
 
 /* ------------------------------------------------------------------------------------ */
+/* Learned tuner network (no counterpart in the reference): I -> H -> H -> K, ReLU, softmax, */
+/* trained with soft cross-entropy and Adam by hand-written CUDA kernels (FP32).          */
+/* It only chooses a schedule; it never changes the SpMV arithmetic.                     */
+/* ------------------------------------------------------------------------------------ */
+typedef struct bhsp_mlp bhsp_mlp;
+int bhsp_mlp_create(bhsp_mlp** out, int n_in, int n_hidden, int n_out, int max_batch);
+/* Flat parameter vector W1[H][I] b1[H] W2[H][H] b2[H] W3[K][H] b3[K] (host copies). */
+size_t bhsp_mlp_num_params(const bhsp_mlp* m);
+int bhsp_mlp_set_params(bhsp_mlp* m, const float* host_params, size_t count);
+int bhsp_mlp_get_params(const bhsp_mlp* m, float* host_params, size_t count);
+/* Inputs are standardised as (f - mean) / std on the device (host arrays of n_in). */
+int bhsp_mlp_set_normalization(bhsp_mlp* m, const float* mean, const float* std);
+/* Probabilities [batch][K] of d_features [batch][I] (device pointers), enqueued on stream. */
+int bhsp_mlp_forward(bhsp_mlp* m, const float* d_features, int batch, float* d_probs, void* stream);
+/* Gradient of the mean soft cross-entropy against d_targets [batch][K] (rows sum to 1) into
+ * d_grads_out (device, num_params; may be NULL) and the loss into *loss_out (host; may be
+ * NULL).  Synchronous. */
+int bhsp_mlp_gradients(bhsp_mlp* m, const float* d_features, const float* d_targets, int batch,
+                       float* d_grads_out, float* loss_out, void* stream);
+/* One Adam step (beta 0.9 / 0.999, decoupled weight decay added to the gradient). */
+int bhsp_mlp_train_step(bhsp_mlp* m, const float* d_features, const float* d_targets, int batch,
+                        float lr, float weight_decay, float* loss_out, void* stream);
+void bhsp_mlp_destroy(bhsp_mlp* m);
+
+/* ------------------------------------------------------------------------------------ */
 /* Allocation-free entry point (no counterpart in the reference).                        */
 /* ------------------------------------------------------------------------------------ */
 /* Size of the fixed device scratch array behind bhsp_spmv_f64_noalloc: 2 MiB, held on every GPU
