@@ -106,6 +106,7 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
     p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
 }
 
+// grid size for n threads in blocks of 256 (every launch below uses 256-thread blocks)
 int blocks_for(long long n) { return (int)((n + 255) / 256); }
 
 }  // namespace
@@ -239,7 +240,7 @@ static cudaError_t mlp_backward(bhsp_mlp* m, const float* d_features, const floa
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(m->loss, 0, sizeof(float), st);
     if (e != cudaSuccess) return e;
-    k_softmax_xent<<<blocks_for(B), 128, 0, st>>>(m->z3, d_targets, B, O, m->p, m->dz3, m->loss);
+    k_softmax_xent<<<blocks_for(B), 256, 0, st>>>(m->z3, d_targets, B, O, m->p, m->dz3, m->loss);
     float* g = m->grads;
     float* gW1 = g;
     float* gb1 = gW1 + H * I;
@@ -262,7 +263,7 @@ extern "C" int bhsp_mlp_forward(bhsp_mlp* m, const float* d_features, int batch,
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = mlp_forward(m, d_features, batch, st);
     if (e == cudaSuccess) {
-        k_softmax_xent<<<blocks_for(batch), 128, 0, st>>>(m->z3, nullptr, batch, m->O, d_probs,
+        k_softmax_xent<<<blocks_for(batch), 256, 0, st>>>(m->z3, nullptr, batch, m->O, d_probs,
                                                           nullptr, nullptr);
         e = cudaGetLastError();
     }

@@ -14,6 +14,7 @@ import sys
 import numpy as np
 
 N_TRAIN = 2000
+EPOCHS, LR, WD = 300, 2e-3, 3e-4
 
 
 def main(data_path: str, out_prefix: str) -> dict:
@@ -23,9 +24,15 @@ def main(data_path: str, out_prefix: str) -> dict:
     f, ms = d["features"][:done], d["ms"][:done]
     ntr = min(N_TRAIN, done - max(done // 11, 1))
     ftr, mtr, fte, mte = f[:ntr], ms[:ntr], f[ntr:], ms[ntr:]
+    # the confidence threshold is calibrated on matrices the network was not fitted on: fit on
+    # 85 % of the training set, calibrate on the other 15 %, then refit on all of it
+    nfit = int(0.85 * ntr)
+    probe = mlp.LearnedTuner(n_out=ms.shape[1], seed=0)
+    probe.fit(ftr[:nfit], mtr[:nfit], epochs=EPOCHS, batch=256, lr=LR, weight_decay=WD)
+    threshold = probe.calibrate_threshold(ftr[nfit:], mtr[nfit:], target=0.97, max_fallback=0.25)
     tuner = mlp.LearnedTuner(n_out=ms.shape[1], seed=0)
-    hist = tuner.fit(ftr, mtr, epochs=400, batch=256, lr=3e-3, weight_decay=1e-4)
-    tuner.calibrate_threshold(ftr, mtr, target=0.97, max_fallback=0.2)
+    hist = tuner.fit(ftr, mtr, epochs=EPOCHS, batch=256, lr=LR, weight_decay=WD)
+    tuner.threshold = threshold
     ev_te = tuner.evaluate(fte, mte)
     ev_tr = tuner.evaluate(ftr, mtr)
     frac_tr = mtr.min(1, keepdims=True) / mtr

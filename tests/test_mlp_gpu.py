@@ -43,10 +43,10 @@ def test_training_learns_a_toy_rule(cuda_ok):
     ms = np.ones((n, K), np.float32) * 2.0
     ms[np.arange(n), best] = 1.0
     tuner = mlp.LearnedTuner(n_out=K, seed=1)
-    hist = tuner.fit(f[:1200], ms[:1200], epochs=60, batch=128, lr=3e-3)
+    hist = tuner.fit(f[:1200], ms[:1200], epochs=120, batch=128, lr=3e-3)
     assert hist[-1] < 0.5 * hist[0]
     ev = tuner.evaluate(f[1200:], ms[1200:])
-    assert ev["mean_frac_without_fallback"] >= 0.9
+    assert ev["mean_frac_without_fallback"] >= 0.9, ev
 
 
 DATA = os.path.join(os.path.dirname(mlp.__file__), "tuner_data")
