@@ -158,6 +158,24 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(seconds: float, dist=None) -> float:
+    """The slowest rank's time: each rank's seconds all-reduced with MAX (a CUDA tensor under
+    NCCL, a host tensor under gloo); the local value when there is no process group."""
+    if dist is None:
+        return seconds
+    import torch
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gbs(world: int, bytes_per_step: int, steps: int, seconds: float) -> float:
+    """Aggregate GB/s of `world` replicas that each moved bytes_per_step * steps bytes, timed by
+    the slowest rank (weak scaling: the per-rank work is fixed)."""
+    return world * bytes_per_step * steps / seconds / 1e9
+
+
 # ---------------------------------------------------------------------------------------
 # reference arm: the reference's CPU path (port) on all host cores
 # ---------------------------------------------------------------------------------------
@@ -290,12 +308,8 @@ def run_ours(args) -> None:
     step_ms = [e0.elapsed_time(e2) for e0, _, e2 in ev]
     kern_ms = [e0.elapsed_time(e1) for e0, e1, _ in ev]
     cal_ms = [e1.elapsed_time(e2) for _, e1, e2 in ev]
-    total_s = sum(step_ms) / 1e3
-    if dist is not None:
-        t = torch.tensor([total_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * B * args.steps / total_s / 1e9
+    total_s = max_over_ranks(sum(step_ms) / 1e3, dist)
+    value = whole_job_gbs(world, B, args.steps, total_s)
 
     # end to end through the C ABI with host buffers (pinned), copies inside the timed region
     x_ptr = x_pin.data_ptr()
@@ -307,9 +321,9 @@ def run_ours(args) -> None:
         assert h.set_x_ptr(x_ptr) == 0, h.last_error
         assert h.run_benchmark() == 0, h.last_error
         assert h.get_y() == 0, h.last_error
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     barrier()
-    e2e_value = world * B * args.steps / e2e_s / 1e9
+    e2e_value = whole_job_gbs(world, B, args.steps, e2e_s)
 
     # correctness of the benchmarked y against the FP64 compensated oracle
     ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)

@@ -134,6 +134,7 @@ struct PolMixedK {
         return r;
     }
     __device__ static Carry carry_from(const Acc& a) { return a; }
+    __device__ static Acc carry_to_acc(const Carry& c) { return c; }
     __device__ static Carry carry_add(const Carry& c, const Acc& a) { return add(c, a); }
     __device__ static YT out_acc(const Acc& a) {
         YT r;

@@ -43,6 +43,7 @@ struct PolMixed {
     __device__ static float2 fma(float v, float x, float2 a) { return ff_add_product(v, x, a); }
     __device__ static float2 add(float2 a, float2 b) { return ff_add(a, b); }
     __device__ static float2 carry_from(float2 a) { return a; }
+    __device__ static float2 carry_to_acc(float2 c) { return c; }
     __device__ static float2 carry_add(float2 c, float2 a) { return ff_add(c, a); }
     __device__ static float out_acc(float2 a) { return __fadd_rn(a.x, a.y); }
     __device__ static float out_carry(float2 c) { return __fadd_rn(c.x, c.y); }

@@ -19,6 +19,7 @@ struct PolF64 {
     __device__ static double add(double a, double b) { return a + b; }
     __device__ static double carry_add(double c, double a) { return c + a; }
     __device__ static double carry_from(double a) { return a; }
+    __device__ static double carry_to_acc(double c) { return c; }
     __device__ static double out_acc(double a) { return a; }
     __device__ static double out_carry(double c) { return c; }
     using Rec = double;
@@ -41,6 +42,7 @@ struct PolF32 {
     __device__ static float add(float a, float b) { return a + b; }
     __device__ static float carry_add(float c, float a) { return c + a; }
     __device__ static float carry_from(float a) { return a; }
+    __device__ static float carry_to_acc(float c) { return c; }
     __device__ static float out_acc(float a) { return a; }
     __device__ static float out_carry(float c) { return c; }
     using Rec = float;

@@ -33,7 +33,7 @@
 // accumulator and within-worker carry, FP64 carry records and calibration).
 //
 // Policy interface: Acc (per-lane accumulator): zero, fma, add; Carry (a worker's open row):
-// carry_zero, carry_add(Carry, Acc), carry_from(Acc), out_carry -> YT; Rec (a carry record
+// carry_zero, carry_add(Carry, Acc), carry_from(Acc), carry_to_acc, out_carry -> YT; Rec (a carry record
 // between workers): rec_from(Carry), rec_add, rec_of_y(YT), out_rec -> YT; out_acc(Acc) -> YT.
 #pragma once
 #include "tile.cuh"
@@ -263,7 +263,11 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
             dc_active = false;
         }
 
+        // A tile with a row head that does not start with one continues carry_row in its first
+        // slots: lane 0's running sum starts from the carry, so the tile's head-less run T0
+        // already holds the whole row (one FP64 add per tile less than adding it afterwards).
         Acc run = fmask ? P::zero() : dc;
+        if (fmask != 0u && !first_head && lane == 0) run = P::carry_to_acc(carry);
         Acc head = P::zero();
         int cur_row = -1;  // row of this lane's open segment
 #pragma unroll
@@ -342,7 +346,7 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
             fin = P::add(run, A);
             if (lane != last) store_row(a.y, a.m, cur_row, P::out_acc(fin), a.err);
         }
-        if (!first_head) flush(carry_row, P::carry_add(carry, T0), carry_owned);  // open row ends
+        if (!first_head) flush(carry_row, P::carry_from(T0), carry_owned);  // open row ends here
         carry_row = __shfl_sync(SPMV_FULL_MASK, cur_row, last);
         carry = P::carry_from(sh_idx(fin, last));
         carry_owned = true;
@@ -356,9 +360,16 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     if (!rec_written && lane == 0) a.rec_row[worker] = -1;
 }
 
+// Resident warps per SM asked of the register allocator: 24 for S = 8 (80 registers, no spills;
+// +4 % on the gather-bound power-law matrix), no request otherwise (S >= 16 would spill).
+template <int S, int WARPS>
+struct MinBlocks {
+    static constexpr int value = S == 8 ? 24 / WARPS : 1;
+};
+
 // One warp = one worker, worker = global warp index (static schedule).
 template <class P, int S, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
     k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
     __shared__ uint32_t s_words[WARPS][32];
     __shared__ int s_rowof[WARPS][32 * S];

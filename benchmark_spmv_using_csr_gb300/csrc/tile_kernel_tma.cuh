@@ -225,6 +225,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         }
 
         Acc run = fmask ? P::zero() : dc;
+        if (fmask != 0u && !first_head && lane == 0) run = P::carry_to_acc(carry);
         Acc head = P::zero();
         int cur_row = -1;  // row of this lane's open segment
         {
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
             fin = P::add(run, A);
             if (lane != last) store_row(a.y, a.m, cur_row, P::out_acc(fin), a.err);
         }
-        if (!first_head) flush(carry_row, P::carry_add(carry, T0), carry_owned);
+        if (!first_head) flush(carry_row, P::carry_from(T0), carry_owned);
         carry_row = __shfl_sync(SPMV_FULL_MASK, cur_row, last);
         carry = P::carry_from(sh_idx(fin, last));
         carry_owned = true;
