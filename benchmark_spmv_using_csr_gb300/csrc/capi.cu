@@ -35,7 +35,7 @@ size_t host_bytes(int vt) { return vt == BHSP_VALUE_F32 ? 4 : 8; }
 bool config_ok(const TileConfig& c, int vt) {
     if (!((c.seg == 8 || c.seg == 16 || c.seg == 32) && c.tiles_per_worker >= 1 &&
           c.tiles_per_worker <= (1 << 20) && (c.warps_per_cta == 4 || c.warps_per_cta == 8) &&
-          (c.stages == 0 || c.stages == 2 || c.stages == 3)))
+          (c.stages == 0 || c.stages == 2 || c.stages == 3 || c.stages == 4)))
         return false;
     const int smem = tile_config_smem_bytes(vt, c);
     return smem >= 0 && smem <= 227 * 1024;

@@ -13,7 +13,7 @@ struct TileConfig {
     int seg;               // S in {8, 16, 32}
     int tiles_per_worker;  // >= 1
     int warps_per_cta;     // 4 or 8
-    int stages;            // 0: direct 256-bit loads; 2 or 3: TMA-staged ring of that depth
+    int stages;            // 0: direct 256-bit loads; 2, 3 or 4: TMA-staged ring of that depth
 };
 
 // partition.cu

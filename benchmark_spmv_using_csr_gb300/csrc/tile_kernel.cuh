@@ -168,6 +168,40 @@ __device__ __forceinline__ void load_vals(const TileArgs<P>& a, int t, int c, in
     }
 }
 
+// T_l = head_l + (has_l ? 0 : T_{l+1}): the head-less run that starts at lane l (the slots
+// before lane l's first row head plus, while lanes have no head, those of the lanes after it).
+// fmask has bit l set when lane l has a row head.  A short chain of shuffles when the longest
+// run of head-less lanes is at most 5, else a 5-step segmented scan.
+template <class P>
+__device__ __forceinline__ typename P::Acc head_run_scan(typename P::Acc head, bool has,
+                                                         uint32_t fmask, int lane) {
+    using Acc = typename P::Acc;
+    Acc T = head;
+    const int D = longest_zero_run(fmask);
+    if (D <= 5) {
+        bool stop = has;
+        for (int d = 1; d <= D; ++d) {
+            const Acc hv = sh_down(head, d);
+            if (!stop && lane + d < 32) {
+                T = P::add(T, hv);
+                stop = ((fmask >> (lane + d)) & 1u) != 0u;
+            }
+        }
+    } else {
+        int stop = has ? 1 : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const Acc tv = sh_down(T, d);
+            const int sv = __shfl_down_sync(SPMV_FULL_MASK, stop, d);
+            if (!stop && lane + d < 32) {
+                T = P::add(T, tv);
+                stop = sv;
+            }
+        }
+    }
+    return T;
+}
+
 // The tile kernel.  One warp = one worker over tiles [t_begin, t_end).  The stream runs as a
 // software pipeline over the worker's chunks of CW non-zeros per lane: while chunk g is
 // multiplied, the values of chunk g+1 and the column indices of chunk g+2 are in flight and the
@@ -314,29 +348,7 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
         const bool has = cur_row >= 0;
         if (!has) head = run;
         // T_l = head_l + (has_l ? 0 : T_{l+1}): the head-less run that starts at lane l
-        Acc T = head;
-        const int D = longest_zero_run(fmask);
-        if (D <= 5) {
-            bool stop = has;
-            for (int d = 1; d <= D; ++d) {
-                const Acc hv = sh_down(head, d);
-                if (!stop && lane + d < 32) {
-                    T = P::add(T, hv);
-                    stop = ((fmask >> (lane + d)) & 1u) != 0u;
-                }
-            }
-        } else {
-            int stop = has ? 1 : 0;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const Acc tv = sh_down(T, d);
-                const int sv = __shfl_down_sync(SPMV_FULL_MASK, stop, d);
-                if (!stop && lane + d < 32) {
-                    T = P::add(T, tv);
-                    stop = sv;
-                }
-            }
-        }
+        const Acc T = head_run_scan<P>(head, has, fmask, lane);
         Acc A = sh_down(T, 1);
         if (lane == 31) A = P::zero();
         const Acc T0 = sh_idx(T, 0);
@@ -360,11 +372,11 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     if (!rec_written && lane == 0) a.rec_row[worker] = -1;
 }
 
-// Resident warps per SM asked of the register allocator: 24 for S = 8 (80 registers, no spills;
-// +4 % on the gather-bound power-law matrix), no request otherwise (S >= 16 would spill).
+// Resident warps per SM asked of the register allocator: 24 for S = 8 (80 registers), 16 for
+// S = 16 (128 registers), no request for S = 32.
 template <int S, int WARPS>
 struct MinBlocks {
-    static constexpr int value = S == 8 ? 24 / WARPS : 1;
+    static constexpr int value = S == 8 ? 24 / WARPS : S == 16 ? 16 / WARPS : 1;
 };
 
 // One warp = one worker, worker = global warp index (static schedule).

@@ -1,24 +1,38 @@
 // tile_kernel_tma.cuh -- the tile kernel with its val / col_idx stream staged in shared
-// memory by bulk (TMA) copies.
+// memory by 2D tensor (TMA) copies.
 //
 // Same algorithm and output as k_tiles (tile_kernel.cuh); what changes is how a tile reaches
 // the lanes:
-//  * every lane issues two cp.async.bulk copies per tile (its S values and its S column
-//    indices) into its own padded run of a per-warp ring of NSTAGE tile slots, completing
-//    on the slot's mbarrier.  The stream therefore runs NSTAGE-1 tiles ahead without holding
-//    any registers, and the padding (16 bytes per run) makes the 16-byte shared-memory reads
-//    of the lane-contiguous runs bank-conflict free;
-//  * x is gathered one chunk of 8 non-zeros ahead of the fused multiply-adds;
-//  * the row of a row head is read from a slot->row map built while the bit flags are
-//    generated (tile_rows below), so dirty tiles (empty rows) need no compaction step;
-//  * tile_ptr and the first 32 row_ptr entries of the next tile's span are prefetched one
-//    tile ahead.
-// Every mbarrier wait is bounded; a timeout sets ERR_WAIT_TIMEOUT, the warp drains the copies
-// it still has in flight (again bounded) and stops.
+//  * val and col_idx are each viewed as a 2D tensor of 128-byte rows; a tile of 32*S
+//    non-zeros is a whole number of rows, so one cp.async.bulk.tensor.2d per array moves the
+//    tile into a slot of a per-warp ring of NSTAGE slots, completing on the slot's mbarrier.
+//    The stream runs NSTAGE-1 tiles ahead of the multiply-adds without holding registers;
+//  * the copies use the 128-byte swizzle (16-byte chunk j of row r lands at chunk j ^ (r & 7)),
+//    which makes the lanes' 16-byte reads of their contiguous runs (64, 128 or 256 bytes
+//    apart) bank-conflict free for runs of up to 128 bytes;
+//  * x is gathered one chunk of 8 non-zeros ahead of the fused multiply-adds, across tile
+//    boundaries (the next tile's slot is waited for during the current tile's last chunk);
+//  * the row of a row head is read from the slot->row map built by tile_rows;
+//  * the matrix's last tile, when partial, is staged by guarded loads into the same layout.
+// Every mbarrier wait is bounded; a timeout sets ERR_WAIT_TIMEOUT, the warp waits (again
+// bounded) for the copies it still has in flight and stops.
 #pragma once
+#include <cuda.h>
+
 #include "tile_kernel.cuh"
 
 namespace spmv {
+
+// The two tensor maps of one launch (val and col_idx as rows of 128 bytes).
+struct StreamMaps {
+    CUtensorMap val;
+    CUtensorMap col;
+};
+
+// Host: encode a map over `bytes` bytes at `base` as floor(bytes / 128) rows of 32 u32 words,
+// box of `box_rows` rows, 128-byte swizzle (tensor_map.cu).  False if the driver rejects it
+// (e.g. a base address that is not 16-byte aligned) or there is no full row.
+bool encode_stream_map(const void* base, long long bytes, int box_rows, CUtensorMap* map);
 
 template <typename VS>
 __device__ __forceinline__ VS zero_value() { return VS(0.0f); }
@@ -29,36 +43,56 @@ template <class P, int S, int NSTAGE>
 struct TmaLayout {
     using VS = typename P::VS;
     static constexpr int TILE = 32 * S;
-    static constexpr int VSTR = S * (int)sizeof(VS) + 16;  // bytes per lane run of values
-    static constexpr int CSTR = S * 4 + 16;                // bytes per lane run of columns
-    static constexpr int SLOT = 32 * VSTR + 32 * CSTR;
+    static constexpr int VBYTES = TILE * (int)sizeof(VS);  // one tile of values
+    static constexpr int CBYTES = TILE * 4;                // one tile of column indices
+    static constexpr int VROWS = VBYTES / 128;             // box heights of the two copies
+    static constexpr int CROWS = CBYTES / 128;
+    static constexpr int VREG = (VBYTES + 1023) / 1024 * 1024;  // swizzle atoms are 1 KB aligned
+    static constexpr int CREG = (CBYTES + 1023) / 1024 * 1024;
+    static constexpr int SLOT = VREG + CREG;
     static constexpr int ROWOF = TILE * 4;
     static constexpr int RAW = NSTAGE * SLOT + ROWOF + 128 + NSTAGE * 8;
-    static constexpr int WARP_BYTES = (RAW + 127) / 128 * 128;
-    static_assert(VSTR % 16 == 0 && CSTR % 16 == 0 && SLOT % 16 == 0, "TMA alignment");
-    static_assert(S * (int)sizeof(VS) % 16 == 0 && S * 4 % 16 == 0, "bulk copy size");
+    static constexpr int WARP_BYTES = (RAW + 1023) / 1024 * 1024;
+    static_assert(VBYTES % 128 == 0 && CBYTES % 128 == 0, "a tile is whole 128-byte rows");
+    static_assert(VROWS <= 256 && CROWS <= 256, "TMA box height");
 };
 
-// 8 values / 8 columns of chunk c from this lane's runs in shared memory (16-byte reads)
-__device__ __forceinline__ void smem_vals8(const unsigned char* run, int c, double (&v)[8]) {
-    const double2* p = reinterpret_cast<const double2*>(run + c * 64);
+// 128-byte swizzle of a byte offset inside a 1 KB-aligned region
+__device__ __forceinline__ uint32_t swz128(uint32_t o) { return o ^ (((o >> 7) & 7u) << 4); }
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar, uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        ".L2::cache_hint [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+}
+
+// 8 values of one chunk: `off` is the logical byte offset of the chunk in the slot's values
+__device__ __forceinline__ void swz_vals8(const unsigned char* base, uint32_t off,
+                                          double (&v)[8], const double*) {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        const double2 d = p[i];
+        const double2 d = *reinterpret_cast<const double2*>(base + swz128(off + 16 * i));
         v[2 * i] = d.x;
         v[2 * i + 1] = d.y;
     }
 }
-__device__ __forceinline__ void smem_vals8(const unsigned char* run, int c, float (&v)[8],
-                                           const float*) {
-    const float4* p = reinterpret_cast<const float4*>(run + c * 32);
-    const float4 a = p[0], b = p[1];
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+__device__ __forceinline__ void swz_vals8(const unsigned char* base, uint32_t off, float (&v)[8],
+                                          const float*) {
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const float4 q = *reinterpret_cast<const float4*>(base + swz128(off + 16 * i));
+        v[4 * i] = q.x;
+        v[4 * i + 1] = q.y;
+        v[4 * i + 2] = q.z;
+        v[4 * i + 3] = q.w;
+    }
 }
-__device__ __forceinline__ void smem_vals8(const unsigned char* run, int c, float (&v)[8],
-                                           const __nv_bfloat16*) {
-    const uint4 q = *reinterpret_cast<const uint4*>(run + c * 16);
+__device__ __forceinline__ void swz_vals8(const unsigned char* base, uint32_t off, float (&v)[8],
+                                          const __nv_bfloat16*) {
+    const uint4 q = *reinterpret_cast<const uint4*>(base + swz128(off));
     const uint32_t w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -66,19 +100,15 @@ __device__ __forceinline__ void smem_vals8(const unsigned char* run, int c, floa
         v[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
     }
 }
-template <typename VS>
-__device__ __forceinline__ void smem_vals(const unsigned char* run, int c, double (&v)[8]) {
-    smem_vals8(run, c, v);
-}
-template <typename VS>
-__device__ __forceinline__ void smem_vals(const unsigned char* run, int c, float (&v)[8]) {
-    smem_vals8(run, c, v, static_cast<const VS*>(nullptr));
-}
-__device__ __forceinline__ void smem_cols8(const unsigned char* run, int c, int (&cc)[8]) {
-    const int4* p = reinterpret_cast<const int4*>(run + c * 32);
-    const int4 a = p[0], b = p[1];
-    cc[0] = a.x; cc[1] = a.y; cc[2] = a.z; cc[3] = a.w;
-    cc[4] = b.x; cc[5] = b.y; cc[6] = b.z; cc[7] = b.w;
+__device__ __forceinline__ void swz_cols8(const unsigned char* base, uint32_t off, int (&c)[8]) {
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const int4 q = *reinterpret_cast<const int4*>(base + swz128(off + 16 * i));
+        c[4 * i] = q.x;
+        c[4 * i + 1] = q.y;
+        c[4 * i + 2] = q.z;
+        c[4 * i + 3] = q.w;
+    }
 }
 
 template <typename XT>
@@ -90,7 +120,8 @@ __device__ __forceinline__ void gather8(const XT* __restrict__ x, const int (&c)
 
 template <class P, int S, int WARPS, int NSTAGE>
 __global__ void __launch_bounds__(WARPS * 32, 1)
-    k_tiles_tma(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
+    k_tiles_tma(TileArgs<P> a, const __grid_constant__ StreamMaps maps, int tpw, int nworkers,
+                int ntiles) {
     using L = TmaLayout<P, S, NSTAGE>;
     using VS = typename P::VS;
     using Acc = typename P::Acc;
@@ -100,19 +131,23 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     using YT = typename P::YT;
     constexpr int TILE = 32 * S;
     constexpr int NC = S / 8;
-    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr uint32_t VRUN = S * sizeof(VS);  // bytes of one lane's values in a tile
+    constexpr uint32_t CRUN = S * 4;
+    extern __shared__ unsigned char smem_raw[];
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int worker = blockIdx.x * WARPS + warp;
     if (worker >= nworkers) return;
+    // the launch reserves 1 KB more than the layout so that the base can be 1 KB aligned
+    unsigned char* const smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     unsigned char* const wb = smem + warp * L::WARP_BYTES;
     int* const rowof = reinterpret_cast<int*>(wb + NSTAGE * L::SLOT);
     uint32_t* const words = reinterpret_cast<uint32_t*>(wb + NSTAGE * L::SLOT + L::ROWOF);
     uint64_t* const bars = reinterpret_cast<uint64_t*>(wb + NSTAGE * L::SLOT + L::ROWOF + 128);
     if (lane == 0) {
 #pragma unroll
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 32);
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
         fence_barrier_init();
     }
     __syncwarp();
@@ -122,25 +157,56 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     const uint64_t pol_s = policy_evict_first();
     const uint64_t pol_x = policy_evict_last();
     auto is_full = [&](int t) { return (long long)(t + 1) * TILE <= a.nnz; };
+    auto vslot = [&](int t) { return wb + ((t - t_begin) % NSTAGE) * L::SLOT; };
 
-    // bulk copies of tile t's runs into its slot (full tiles only)
-    int issued = t_begin;  // tiles [t_begin, issued) have been issued (or staged later)
+    // tensor copies of tile t's values and columns into its slot (full tiles only)
+    int issued = t_begin;  // tiles [t_begin, issued) have been issued (or are staged by hand)
     auto issue_next = [&]() {
         const int t = issued;
         if (t >= t_end) return;
         ++issued;
-        if (!is_full(t)) return;
+        if (!is_full(t) || lane != 0) return;
         const int s = (t - t_begin) % NSTAGE;
         unsigned char* sl = wb + s * L::SLOT;
-        const int e = t * TILE + lane * S;
-        mbar_arrive_expect_tx(&bars[s], (uint32_t)(S * sizeof(VS) + S * 4));
-        bulk_g2s(sl + lane * L::VSTR, a.val + e, (uint32_t)(S * sizeof(VS)), &bars[s], pol_s);
-        bulk_g2s(sl + 32 * L::VSTR + lane * L::CSTR, a.col + e, (uint32_t)(S * 4), &bars[s], pol_s);
+        mbar_arrive_expect_tx(&bars[s], (uint32_t)(L::VBYTES + L::CBYTES));
+        tma_load_2d(sl, &maps.val, 0, t * L::VROWS, &bars[s], pol_s);
+        tma_load_2d(sl + L::VREG, &maps.col, 0, t * L::CROWS, &bars[s], pol_s);
     };
+    // make tile t's slot readable: wait for its copies, or stage the partial last tile
+    auto ready = [&](int t) -> bool {
+        if (is_full(t)) {
+            const int s = (t - t_begin) % NSTAGE;
+            const uint32_t parity = (uint32_t)((t - t_begin) / NSTAGE) & 1u;
+            return mbar_wait_bounded(&bars[s], parity);
+        }
+        unsigned char* sl = vslot(t);
+        const int e0 = t * TILE;
+#pragma unroll 4
+        for (int k = 0; k < S; ++k) {
+            const int e = e0 + lane * S + k;
+            const bool in = e < a.nnz;
+            *reinterpret_cast<VS*>(sl + swz128(lane * VRUN + k * sizeof(VS))) =
+                in ? a.val[e] : zero_value<VS>();
+            *reinterpret_cast<int*>(sl + L::VREG + swz128(lane * CRUN + k * 4)) = in ? a.col[e] : -1;
+        }
+        __syncwarp();
+        return true;
+    };
+    auto gather_chunk = [&](int t, int c, XT (&xv)[8]) {
+        int cc[8];
+        swz_cols8(vslot(t) + L::VREG, lane * CRUN + c * 32, cc);
+        gather8(a.x, cc, pol_x, xv);
+    };
+
 #pragma unroll
     for (int i = 0; i < NSTAGE - 1; ++i) issue_next();
-    uint32_t parity = 0u;
     int t_fail = -1;  // tile whose wait timed out
+    XT xa[8];
+    if (!ready(t_begin)) {
+        t_fail = t_begin;
+    } else {
+        gather_chunk(t_begin, 0, xa);
+    }
 
     uint32_t tp0 = __ldg(a.tile_ptr + t_begin);
     uint32_t tp1 = __ldg(a.tile_ptr + t_begin + 1);
@@ -164,7 +230,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         if (!owned) rec_written = true;
     };
 
-    for (int t = t_begin; t < t_end; ++t) {
+    for (int t = t_begin; t < t_end && t_fail < 0; ++t) {
         issue_next();  // tile t+NSTAGE-1 into the slot that tile t-1 has released
         const int lo = (int)(tp0 & ROW_MASK);
         const int hi = (int)(tp1 & ROW_MASK);
@@ -174,8 +240,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
             tp2 = __ldg(a.tile_ptr + t + 2);
             rbn = prefetch_rows(a.row_ptr, a.m, hi);
         }
-        const int e0 = t * TILE;
-        const uint32_t w = tile_rows<S, YT>(a.row_ptr, a.m, e0, lo, hi, rb, words, rowof, a.y);
+        const uint32_t w = tile_rows<S, YT>(a.row_ptr, a.m, t * TILE, lo, hi, rb, words, rowof, a.y);
         const bool first_head = ((__shfl_sync(SPMV_FULL_MASK, w, 0) >> 31) & 1u) != 0u;
         const uint32_t fmask = __ballot_sync(SPMV_FULL_MASK, w != 0u);
 
@@ -200,71 +265,44 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
             dc_active = false;
         }
 
-        // the tile's data in its slot
-        const int s = (t - t_begin) % NSTAGE;
-        unsigned char* sl = wb + s * L::SLOT;
-        unsigned char* vrun = sl + lane * L::VSTR;
-        unsigned char* crun = sl + 32 * L::VSTR + lane * L::CSTR;
-        if (is_full(t)) {
-            if (!mbar_wait_bounded(&bars[s], (parity >> s) & 1u)) {
-                t_fail = t;
-                if (lane == 0) atomicOr(a.err, ERR_WAIT_TIMEOUT);
-                break;
-            }
-            parity ^= 1u << s;
-        } else {
-            // the matrix's last, partial tile: staged with guarded loads, zero padded
-#pragma unroll 4
-            for (int k = 0; k < S; ++k) {
-                const int e = e0 + lane * S + k;
-                const bool in = e < a.nnz;
-                reinterpret_cast<VS*>(vrun)[k] = in ? a.val[e] : zero_value<VS>();
-                reinterpret_cast<int*>(crun)[k] = in ? a.col[e] : -1;
-            }
-            __syncwarp();
-        }
-
+        const unsigned char* vsl = vslot(t);
         Acc run = fmask ? P::zero() : dc;
         if (fmask != 0u && !first_head && lane == 0) run = P::carry_to_acc(carry);
         Acc head = P::zero();
         int cur_row = -1;  // row of this lane's open segment
-        {
-            int cc[8];
-            XT xa[8];
-            smem_cols8(crun, 0, cc);
-            gather8(a.x, cc, pol_x, xa);
 #pragma unroll
-            for (int c = 0; c < NC; ++c) {
-                XT xb[8];
-                if (c + 1 < NC) {
-                    smem_cols8(crun, c + 1, cc);
-                    gather8(a.x, cc, pol_x, xb);
-                }
-                VC v[8];
-                smem_vals<VS>(vrun, c, v);
-                if (fmask == 0u) {
+        for (int c = 0; c < NC; ++c) {
+            XT xb[8];
+            if (c + 1 < NC) {
+                gather_chunk(t, c + 1, xb);
+            } else if (t + 1 < t_end) {  // the next tile's first chunk
+                if (ready(t + 1))
+                    gather_chunk(t + 1, 0, xb);
+                else
+                    t_fail = t + 1;
+            }
+            VC v[8];
+            swz_vals8(vsl, lane * VRUN + c * 8 * sizeof(VS), v, static_cast<const VS*>(nullptr));
+            if (fmask == 0u) {
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) run = P::fma(v[k], xa[k], run);
-                } else {
+                for (int k = 0; k < 8; ++k) run = P::fma(v[k], xa[k], run);
+            } else {
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) {
-                        const int kk = c * 8 + k;
-                        if ((w >> (31 - kk)) & 1u) {
-                            if (cur_row >= 0)
-                                store_row(a.y, a.m, cur_row, P::out_acc(run), a.err);
-                            else
-                                head = run;
-                            cur_row = rowof[lane * S + kk];
-                            run = P::zero();
-                        }
-                        run = P::fma(v[k], xa[k], run);
+                for (int k = 0; k < 8; ++k) {
+                    const int kk = c * 8 + k;
+                    if ((w >> (31 - kk)) & 1u) {
+                        if (cur_row >= 0)
+                            store_row(a.y, a.m, cur_row, P::out_acc(run), a.err);
+                        else
+                            head = run;
+                        cur_row = rowof[lane * S + kk];
+                        run = P::zero();
                     }
-                }
-                if (c + 1 < NC) {
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) xa[k] = xb[k];
+                    run = P::fma(v[k], xa[k], run);
                 }
             }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) xa[k] = xb[k];
         }
         fence_proxy_async();  // this lane's reads of the slot come before the TMA that reuses it
         __syncwarp();
@@ -279,29 +317,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         }
         const bool has = cur_row >= 0;
         if (!has) head = run;
-        Acc T = head;
-        const int D = longest_zero_run(fmask);
-        if (D <= 5) {
-            bool stop = has;
-            for (int d = 1; d <= D; ++d) {
-                const Acc hv = sh_down(head, d);
-                if (!stop && lane + d < 32) {
-                    T = P::add(T, hv);
-                    stop = ((fmask >> (lane + d)) & 1u) != 0u;
-                }
-            }
-        } else {
-            int stop = has ? 1 : 0;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const Acc tv = sh_down(T, d);
-                const int sv = __shfl_down_sync(SPMV_FULL_MASK, stop, d);
-                if (!stop && lane + d < 32) {
-                    T = P::add(T, tv);
-                    stop = sv;
-                }
-            }
-        }
+        const Acc T = head_run_scan<P>(head, has, fmask, lane);
         Acc A = sh_down(T, 1);
         if (lane == 31) A = P::zero();
         const Acc T0 = sh_idx(T, 0);
@@ -318,12 +334,16 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     }
 
     if (t_fail >= 0) {
-        // drain: the copies of tiles [t_fail, issued) are still in flight; each must land
-        // (bounded wait) before the warp's shared memory is released
+        // the copies of tiles [t_fail, issued) may still be in flight; each must land (bounded
+        // wait) before the warp's shared memory is released
+        if (lane == 0) {
+            atomicOr(a.err, ERR_WAIT_TIMEOUT);
+            if (!rec_written) a.rec_row[worker] = -1;
+        }
         for (int t = t_fail; t < issued; ++t) {
             if (!is_full(t)) continue;
             const int s = (t - t_begin) % NSTAGE;
-            mbar_wait_bounded(&bars[s], (parity >> s) & 1u);
+            mbar_wait_bounded(&bars[s], (uint32_t)((t - t_begin) / NSTAGE) & 1u);
         }
         return;
     }
@@ -339,9 +359,19 @@ template <class P, int S, int WARPS, int NSTAGE>
 cudaError_t launch_tiles_tma_t(const TileArgs<P>& a, int tpw, int nworkers, int ntiles,
                                cudaStream_t st) {
     using L = TmaLayout<P, S, NSTAGE>;
-    const int bytes = WARPS * L::WARP_BYTES;
+    const int bytes = WARPS * L::WARP_BYTES + 1024;
     if (bytes > 227 * 1024) return cudaErrorInvalidValue;
     if (nworkers > 0 && (a.phase & 1)) {
+        StreamMaps maps;
+        const long long vbytes = (long long)a.nnz * (long long)sizeof(typename P::VS);
+        if (a.nnz < 32 * S ||
+            !encode_stream_map(a.val, vbytes, L::VROWS, &maps.val) ||
+            !encode_stream_map(a.col, (long long)a.nnz * 4, L::CROWS, &maps.col)) {
+            // no full tile, or a stream the tensor unit cannot address (not 16-byte aligned):
+            // the direct-load kernel with the same tile size
+            TileConfig c{S, tpw, WARPS, 0};
+            return launch_tiles<P>(a, c, st);
+        }
         // the shared-memory opt-in is a per-device function attribute: set it once per device
         static unsigned long long attr_set = 0ull;
         int dev = 0;
@@ -355,7 +385,8 @@ cudaError_t launch_tiles_tma_t(const TileArgs<P>& a, int tpw, int nworkers, int 
             attr_set |= bit;
         }
         const int blocks = (nworkers + WARPS - 1) / WARPS;
-        k_tiles_tma<P, S, WARPS, NSTAGE><<<blocks, WARPS * 32, bytes, st>>>(a, tpw, nworkers, ntiles);
+        k_tiles_tma<P, S, WARPS, NSTAGE>
+            <<<blocks, WARPS * 32, bytes, st>>>(a, maps, tpw, nworkers, ntiles);
     }
     if (a.phase & 2) {
         int cb = (nworkers + 255) / 256;
@@ -374,16 +405,19 @@ int tma_smem_bytes(const TileConfig& c) {
     switch (c.seg * 10 + c.stages) {
         case 82: per_warp = TmaLayout<P, 8, 2>::WARP_BYTES; break;
         case 83: per_warp = TmaLayout<P, 8, 3>::WARP_BYTES; break;
+        case 84: per_warp = TmaLayout<P, 8, 4>::WARP_BYTES; break;
         case 162: per_warp = TmaLayout<P, 16, 2>::WARP_BYTES; break;
         case 163: per_warp = TmaLayout<P, 16, 3>::WARP_BYTES; break;
+        case 164: per_warp = TmaLayout<P, 16, 4>::WARP_BYTES; break;
         case 322: per_warp = TmaLayout<P, 32, 2>::WARP_BYTES; break;
         case 323: per_warp = TmaLayout<P, 32, 3>::WARP_BYTES; break;
+        case 324: per_warp = TmaLayout<P, 32, 4>::WARP_BYTES; break;
         default: return -1;
     }
-    return per_warp * c.warps_per_cta;
+    return per_warp * c.warps_per_cta + 1024;
 }
 
-// Direct-load kernel (stages == 0) or TMA-staged kernel (stages 2 or 3).
+// Direct-load kernel (stages == 0) or TMA-staged kernel (stages 2, 3 or 4).
 template <class P>
 cudaError_t launch_tiles_any(const TileArgs<P>& a, const TileConfig& cfg, cudaStream_t st) {
     if (cfg.stages == 0) return launch_tiles<P>(a, cfg, st);
@@ -391,13 +425,19 @@ cudaError_t launch_tiles_any(const TileArgs<P>& a, const TileConfig& cfg, cudaSt
     const int tpw = cfg.tiles_per_worker;
     const int nw = (nt + tpw - 1) / tpw;
     const bool w8 = cfg.warps_per_cta == 8;
-    const bool s3 = cfg.stages == 3;
+#define SPMV_TMA_STAGES(SEG, W)                                                                    \
+    switch (cfg.stages) {                                                                          \
+        case 2: return launch_tiles_tma_t<P, SEG, W, 2>(a, tpw, nw, nt, st);                       \
+        case 3: return launch_tiles_tma_t<P, SEG, W, 3>(a, tpw, nw, nt, st);                       \
+        case 4: return launch_tiles_tma_t<P, SEG, W, 4>(a, tpw, nw, nt, st);                       \
+        default: return cudaErrorInvalidValue;                                                     \
+    }
 #define SPMV_TMA_CASE(SEG)                                                                         \
     case SEG:                                                                                      \
-        if (w8) return s3 ? launch_tiles_tma_t<P, SEG, 8, 3>(a, tpw, nw, nt, st)                   \
-                          : launch_tiles_tma_t<P, SEG, 8, 2>(a, tpw, nw, nt, st);                  \
-        return s3 ? launch_tiles_tma_t<P, SEG, 4, 3>(a, tpw, nw, nt, st)                           \
-                  : launch_tiles_tma_t<P, SEG, 4, 2>(a, tpw, nw, nt, st);
+        if (w8) {                                                                                  \
+            SPMV_TMA_STAGES(SEG, 8)                                                                \
+        }                                                                                          \
+        SPMV_TMA_STAGES(SEG, 4)
     switch (cfg.seg) {
         SPMV_TMA_CASE(8)
         SPMV_TMA_CASE(16)
@@ -406,6 +446,7 @@ cudaError_t launch_tiles_any(const TileArgs<P>& a, const TileConfig& cfg, cudaSt
             return cudaErrorInvalidValue;
     }
 #undef SPMV_TMA_CASE
+#undef SPMV_TMA_STAGES
 }
 
 }  // namespace spmv

@@ -17,9 +17,10 @@ from benchmark_spmv_using_csr_gb300 import gen
 pytestmark = pytest.mark.gpu
 
 # (non-zeros per lane, tiles per worker, warps per CTA, stages): direct loads (0 stages) and
-# the TMA-staged ring (2 or 3 stages)
+# the TMA-staged ring (2, 3 or 4 stages)
 CONFIGS = [(8, 1, 4, 0), (8, 3, 8, 0), (16, 1, 8, 0), (16, 5, 4, 0), (32, 1, 4, 0), (32, 9, 4, 0),
-           (8, 1, 4, 2), (8, 7, 8, 3), (16, 2, 4, 3), (16, 4, 8, 2), (32, 3, 4, 2), (32, 1, 4, 3)]
+           (8, 1, 4, 2), (8, 7, 8, 3), (16, 2, 4, 3), (16, 4, 8, 2), (32, 3, 4, 2), (32, 1, 4, 3),
+           (8, 5, 4, 4), (16, 3, 4, 4)]
 
 
 def run_handle(vt, rp, col, val, x, cfg=None, y0=None, repeat=1):
