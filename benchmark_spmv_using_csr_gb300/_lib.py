@@ -1,5 +1,5 @@
-"""ctypes binding of ``libspmv_gb300.so`` (the C ABI of include/spmv_gb300.h and
-include/spmv_gen.h).
+"""ctypes binding of ``libspmv_gb300.so`` (the C ABI of include/spmv_gb300.h,
+include/spmv_gen.h and include/spmv_mtx.h).
 
 The library is built in-tree by :mod:`benchmark_spmv_using_csr_gb300.build`.  If it
 is missing this module raises at load time: there is no fallback path.
@@ -105,6 +105,13 @@ SIGNATURES = {
     "bhsp_gen_blockdiag_rows": (c_int64, [c_int, c_int, c_int, c_void_p]),
     "bhsp_gen_blockdiag_fill": (c_int, [c_int, c_int, c_int, c_double, c_double, c_uint64,
                                         c_void_p, c_void_p, c_void_p]),
+    # Matrix Market loading (spmv_mtx.h)
+    "bhsp_mtx_load": (c_int, [c_char_p, P_void]),
+    "bhsp_mtx_get_info": (c_int, [c_void_p, c_void_p]),
+    "bhsp_mtx_row_ptr": (c_void_p, [c_void_p]),
+    "bhsp_mtx_col_idx": (c_void_p, [c_void_p]),
+    "bhsp_mtx_val": (c_void_p, [c_void_p]),
+    "bhsp_mtx_free": (None, [c_void_p]),
 }
 
 
