@@ -371,10 +371,12 @@ def run_ours(args) -> None:
 
     if rank == 0 and args.forms:
         line["forms"] = measure_forms(args, a, x, ystar)
+        line["comparators"] = measure_comparators(args, a, x, ystar)
     if rank == 0 and args.batched:
         line["batched"] = measure_batched(args)
     if rank == 0 and args.cpu_baseline > 0:
         line["cpu_baseline"] = cpu_baseline(a, x, B, args.cpu_baseline)
+        line["cpu_baseline"]["openmp"] = cpu_openmp(a, x, B, max(1.0, args.cpu_baseline / 5))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -421,6 +423,77 @@ def measure_forms(args, a, x, ystar) -> dict:
             "gnnz_per_s": round(a.nnz / (ms * 1e-3) / 1e9, 2),
             "normwise_err_vs_fp64_oracle": oracle.normwise_error(y, ystar)}
         h.close()
+    return out
+
+
+def measure_comparators(args, a, x, ystar) -> dict:
+    """The reference driver's GPU comparators on the same FP64 matrix (include/spmv_compare.h):
+    the CSR-vector kernel with the CUSP schedule and cuSPARSE's generic SpMV, each timed like
+    the headline (L2 flushed before every launch, CUDA events, same algorithmic bytes)."""
+    import numpy as np
+    import torch
+
+    import benchmark_spmv_using_csr_gb300 as sp
+    import oracle
+    from benchmark_spmv_using_csr_gb300 import compare
+    rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
+    val, xd = torch.from_numpy(a.val).cuda(), torch.from_numpy(x).cuda()
+    y = torch.zeros(a.m, dtype=torch.float64, device="cuda")
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    B = alg_bytes(a.m, a.n, a.nnz, 8, 8, 8)
+    steps = max(10, min(args.steps, 50))
+    scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, x)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        evs = []
+        for i in range(steps):
+            flush.fill_(i & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in evs)
+        err = oracle.componentwise_error(y.cpu().numpy(), ystar, scale)
+        return {"gbs": round(B / (ms * 1e-3) / 1e9, 1), "ms_per_step": round(ms, 5),
+                "componentwise_err_vs_fp64_oracle": err}
+
+    out = {}
+    tpv = compare.vector_width(a.m, a.nnz)
+    out["csr_vector"] = timed(lambda: compare.csr_vector(sp.VALUE_F64, rp, ci, val, xd, y, tpv))
+    out["csr_vector"]["threads_per_row"] = tpv
+    try:
+        cs = compare.Cusparse(sp.VALUE_F64, rp, ci, val, xd, y)
+        out["cusparse_spmv_csr_alg1"] = timed(cs.run)
+        cs.close()
+    except RuntimeError as e:
+        out["cusparse_spmv_csr_alg1"] = {"unavailable": str(e)}
+    del rp, ci, val, xd, y, flush
+    torch.cuda.empty_cache()
+    return out
+
+
+def cpu_openmp(a, x, B, seconds: float) -> dict:
+    """The reference's OpenMP CSR loop (spmv_cuda/main.cu:377-393, C port) at its 4 threads
+    (main.cu:370) and at every host thread, whole-matrix passes for about `seconds` each."""
+    import numpy as np
+    import oracle
+    y = np.zeros(a.m)
+    out = {}
+    for label, threads in (("threads_4", 4), ("threads_all", os.cpu_count() or 1)):
+        passes = 0
+        t0 = time.perf_counter()
+        while True:
+            oracle.csr_omp(a.row_ptr, a.col, a.val, x, threads, y=y)
+            passes += 1
+            el = time.perf_counter() - t0
+            if el >= seconds:
+                break
+        out[label] = {"value": round(B * passes / el / 1e9, 3), "unit": UNIT, "cores": threads,
+                      "passes": passes}
     return out
 
 

@@ -1,5 +1,5 @@
 """ctypes binding of ``libspmv_gb300.so`` (the C ABI of include/spmv_gb300.h,
-include/spmv_gen.h and include/spmv_mtx.h).
+include/spmv_gen.h, include/spmv_mtx.h and include/spmv_compare.h).
 
 The library is built in-tree by :mod:`benchmark_spmv_using_csr_gb300.build`.  If it
 is missing this module raises at load time: there is no fallback path.
@@ -112,6 +112,14 @@ SIGNATURES = {
     "bhsp_mtx_col_idx": (c_void_p, [c_void_p]),
     "bhsp_mtx_val": (c_void_p, [c_void_p]),
     "bhsp_mtx_free": (None, [c_void_p]),
+    # comparators (spmv_compare.h)
+    "bhsp_csr_vector_width": (c_int, [c_int, c_int]),
+    "bhsp_csr_vector": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_int, c_void_p]),
+    "bhsp_cusparse_create": (c_int, [P_void, c_int, c_int, c_int, c_int, c_void_p, c_void_p,
+                                     c_void_p, c_void_p, c_void_p, c_void_p]),
+    "bhsp_cusparse_run": (c_int, [c_void_p]),
+    "bhsp_cusparse_destroy": (None, [c_void_p]),
 }
 
 

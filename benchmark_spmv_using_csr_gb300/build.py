@@ -25,7 +25,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-fop
                      "--expt-relaxed-constexpr", "-I" + INCLUDE]
 # extra -D flags for experiments (e.g. SPMV_NVCC_DEFINES="-DSPMV_CACHE_MODE=1")
 NVCC_FLAGS += os.environ.get("SPMV_NVCC_DEFINES", "").split()
-LINK_FLAGS = ["-shared", "-Xcompiler", "-fopenmp", "-lgomp"]
+LINK_FLAGS = ["-shared", "-Xcompiler", "-fopenmp", "-lgomp", "-ldl"]
 
 
 def _nvcc() -> str:
@@ -66,8 +66,30 @@ def _compile(nvcc: str, src: str, verbose: bool) -> str:
     return obj
 
 
+DRIVER_SRC = os.path.join(HERE, "driver", "spmv_main.cpp")
+# the reference-style benchmark driver, one executable per value type (USE_DOUBLE)
+DRIVERS = {"spmv": 1, "spmv_f32": 0}
+
+
+def _build_drivers(nvcc: str, verbose: bool) -> None:
+    incs = [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    for name, use_double in DRIVERS.items():
+        exe = os.path.join(HERE, name)
+        if not _stale(exe, [DRIVER_SRC, LIB_PATH] + incs):
+            continue
+        cmd = [nvcc, "-x", "c++", "-O3", "-std=c++17", "-Xcompiler", "-fopenmp",
+               f"-DUSE_DOUBLE={use_double}", "-I" + INCLUDE, DRIVER_SRC, "-o", exe + ".tmp",
+               "-L" + HERE, "-lspmv_gb300", "-lgomp", "-Xlinker", "-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(exe + ".tmp", exe)
+
+
 def build(verbose: bool = False) -> str:
-    """Compile and link the library; returns its path."""
+    """Compile and link the library and the benchmark driver; returns the library's path."""
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
     srcs = _sources()
@@ -81,6 +103,7 @@ def build(verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(LIB_PATH + ".tmp", LIB_PATH)
+    _build_drivers(nvcc, verbose)
     return LIB_PATH
 
 
