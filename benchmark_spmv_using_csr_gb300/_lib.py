@@ -38,6 +38,7 @@ SIGNATURES = {
     "bhsp_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
     "bhsp_get_config": (c_int, [c_void_p, P_int, P_int, P_int, P_int]),
     "bhsp_set_x": (c_int, [c_void_p, c_void_p]),
+    "bhsp_run_stream": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "bhsp_run_async": (c_int, [c_void_p, c_void_p]),
     "bhsp_check": (c_int, [c_void_p]),
     "bhsp_run_phase": (c_int, [c_void_p, c_void_p, c_int]),

@@ -136,6 +136,17 @@ class BhsparseSpmvCuda:
         """set_x from a raw host address (e.g. pinned memory); the caller keeps it alive."""
         return self._L.bhsp_set_x(self._h, ctypes.c_void_p(ptr))
 
+    def run_stream(self, x_ptrs, y_ptrs) -> int:
+        """bhsp_run_stream: y_ptrs[i] = A x_ptrs[i] for every pair of host addresses (pinned
+        memory in the handle's value type; the caller keeps it alive), with the copies of
+        neighbouring right-hand sides overlapping each SpMV."""
+        if len(x_ptrs) != len(y_ptrs):
+            raise ValueError("x_ptrs and y_ptrs differ in length")
+        k = len(x_ptrs)
+        xs = (ctypes.c_void_p * max(k, 1))(*[ctypes.c_void_p(int(p)) for p in x_ptrs])
+        ys = (ctypes.c_void_p * max(k, 1))(*[ctypes.c_void_p(int(p)) for p in y_ptrs])
+        return self._L.bhsp_run_stream(self._h, k, xs, ys)
+
     def run_async(self, stream: int = 0) -> int:
         return self._L.bhsp_run_async(self._h, ctypes.c_void_p(stream))
 

@@ -377,6 +377,13 @@ struct bhsp_spmv {
     cudaStream_t stream = nullptr;  // stream used by run_benchmark / set_x / get_y
     std::string last_error;
     std::string device_name;
+    // bhsp_run_stream: a second x / y pair (the first is d_x / d_y), an upload, a compute and a
+    // download stream, and per-buffer events; created on first use
+    void* d_x1 = nullptr;
+    void* d_y1 = nullptr;
+    cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
+    cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr},
+                ev_out[2] = {nullptr, nullptr};
 };
 
 static int h_fail(bhsp_spmv* h, int code, const std::string& msg) {
@@ -438,7 +445,29 @@ extern "C" int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tpw, int* warp
     return BHSPARSE_SUCCESS;
 }
 
+static void stream_release(bhsp_spmv* h) {
+    cudaFree(h->d_x1);
+    cudaFree(h->d_y1);
+    h->d_x1 = h->d_y1 = nullptr;
+    for (int i = 0; i < 2; ++i) {
+        if (h->ev_in[i]) cudaEventDestroy(h->ev_in[i]);
+        if (h->ev_comp[i]) cudaEventDestroy(h->ev_comp[i]);
+        if (h->ev_out[i]) cudaEventDestroy(h->ev_out[i]);
+        h->ev_in[i] = h->ev_comp[i] = h->ev_out[i] = nullptr;
+    }
+    if (h->s_in) cudaStreamDestroy(h->s_in);
+    if (h->s_comp) cudaStreamDestroy(h->s_comp);
+    if (h->s_out) cudaStreamDestroy(h->s_out);
+    h->s_in = h->s_comp = h->s_out = nullptr;
+}
+
 static void handle_release(bhsp_spmv* h) {
+    if (h->s_comp) {
+        cudaStreamSynchronize(h->s_in);
+        cudaStreamSynchronize(h->s_comp);
+        cudaStreamSynchronize(h->s_out);
+    }
+    stream_release(h);
     if (h->plan) bhsp_plan_destroy(h->plan);
     h->plan = nullptr;
     cudaFree(h->d_row_ptr);
@@ -577,6 +606,76 @@ extern "C" int bhsp_get_y(bhsp_spmv* h) {
     }
     H_CUDA(h, cudaStreamSynchronize(h->stream));
     return BHSPARSE_SUCCESS;
+}
+
+// Buffers, streams and events of bhsp_run_stream, created once per prepared matrix.
+static int stream_setup(bhsp_spmv* h) {
+    if (h->s_comp) return BHSPARSE_SUCCESS;
+    const size_t vb = vec_bytes(h->vt);
+    H_CUDA(h, cudaMalloc(&h->d_x1, vb * (size_t)(h->n > 0 ? h->n : 1)));
+    H_CUDA(h, cudaMalloc(&h->d_y1, vb * (size_t)(h->m > 0 ? h->m : 1)));
+    H_CUDA(h, cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking));
+    H_CUDA(h, cudaStreamCreateWithFlags(&h->s_comp, cudaStreamNonBlocking));
+    H_CUDA(h, cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+        H_CUDA(h, cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming));
+        H_CUDA(h, cudaEventCreateWithFlags(&h->ev_comp[i], cudaEventDisableTiming));
+        H_CUDA(h, cudaEventCreateWithFlags(&h->ev_out[i], cudaEventDisableTiming));
+    }
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_run_stream(bhsp_spmv* h, int count, const void* const* x_host,
+                               void* const* y_host) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (!h->prepared) return h_fail(h, BHSPARSE_NOT_PREPARED, "run_stream before prepare_mem");
+    if (h->vt != BHSP_VALUE_F64 && h->vt != BHSP_VALUE_F32)
+        return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "run_stream supports the F64 and F32 forms");
+    if (count < 0 || (count > 0 && (!x_host || !y_host)))
+        return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "bad count or null vector list");
+    for (int i = 0; i < count; ++i)
+        if ((h->n > 0 && !x_host[i]) || (h->m > 0 && !y_host[i]))
+            return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "null host vector");
+    H_CUDA(h, cudaSetDevice(h->device));
+    int rc = stream_setup(h);
+    if (rc) return rc;
+    H_CUDA(h, cudaStreamSynchronize(h->stream));  // the handle's own work comes first
+    const size_t vb = vec_bytes(h->vt);
+    void* X[2] = {h->d_x, h->d_x1};
+    void* Y[2] = {h->d_y, h->d_y1};
+    for (int i = 0; i < count; ++i) {
+        const int b = i & 1;
+        // x_i into X[b] once the SpMV of i-2 has read it
+        if (i >= 2) H_CUDA(h, cudaStreamWaitEvent(h->s_in, h->ev_comp[b], 0));
+        if (h->n > 0)
+            H_CUDA(h, cudaMemcpyAsync(X[b], x_host[i], vb * (size_t)h->n, cudaMemcpyHostToDevice,
+                                      h->s_in));
+        H_CUDA(h, cudaEventRecord(h->ev_in[b], h->s_in));
+        // y_i = A x_i once x_i has landed and y_{i-2} has left Y[b]
+        H_CUDA(h, cudaStreamWaitEvent(h->s_comp, h->ev_in[b], 0));
+        if (i >= 2) H_CUDA(h, cudaStreamWaitEvent(h->s_comp, h->ev_out[b], 0));
+        rc = bhsp_plan_execute(h->plan, h->d_val, X[b], Y[b], h->s_comp);
+        if (rc) {
+            h->last_error = h->plan->last_error;
+            cudaStreamSynchronize(h->s_in);
+            cudaStreamSynchronize(h->s_comp);
+            cudaStreamSynchronize(h->s_out);
+            return rc;
+        }
+        H_CUDA(h, cudaEventRecord(h->ev_comp[b], h->s_comp));
+        // y_i to the host
+        H_CUDA(h, cudaStreamWaitEvent(h->s_out, h->ev_comp[b], 0));
+        if (h->m > 0)
+            H_CUDA(h, cudaMemcpyAsync(y_host[i], Y[b], vb * (size_t)h->m, cudaMemcpyDeviceToHost,
+                                      h->s_out));
+        H_CUDA(h, cudaEventRecord(h->ev_out[b], h->s_out));
+    }
+    H_CUDA(h, cudaStreamSynchronize(h->s_in));
+    H_CUDA(h, cudaStreamSynchronize(h->s_comp));
+    H_CUDA(h, cudaStreamSynchronize(h->s_out));
+    rc = plan_check(h->plan, h->s_comp);
+    if (rc) h->last_error = h->plan->last_error;
+    return rc;
 }
 
 extern "C" int bhsp_free_mem(bhsp_spmv* h) {

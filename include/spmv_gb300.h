@@ -94,6 +94,13 @@ int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tiles_per_worker, int* wa
                     int* stages);
 /* Replace x (host pointer, same type as in prepare_mem) without rebuilding anything. */
 int bhsp_set_x(bhsp_spmv* h, const void* x);
+/* Streamed SpMVs over many right-hand sides held in host memory: y_host[i] = A x_host[i] for
+ * i = 0..count-1, with the upload of x_{i+1} and the download of y_{i-1} overlapping the SpMV of
+ * x_i (two device x / y buffers, separate upload, compute and download streams).  Blocks until
+ * every y_host[i] is written.  F64 and F32 forms; host vectors in the handle's value type,
+ * pinned (cudaHostAlloc / cudaHostRegister) for the copies to overlap.  No counterpart in the
+ * reference, whose driver runs one SpMV per prepared x (spmv_cuda/main.cu:811-817). */
+int bhsp_run_stream(bhsp_spmv* h, int count, const void* const* x_host, void* const* y_host);
 /* Enqueue y = A.x on `stream` (a cudaStream_t, NULL = the legacy default stream) and
  * return at once; bhsp_check() synchronises and reports a kernel-side failure. */
 int bhsp_run_async(bhsp_spmv* h, void* stream);

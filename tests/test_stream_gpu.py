@@ -1,0 +1,72 @@
+"""bhsp_run_stream: many right-hand sides from host memory with overlapped copies, against the
+per-call sequence set_x / run_benchmark / get_y and the oracle; the F64 and F32 forms."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import TOL_F64
+
+import benchmark_spmv_using_csr_gb300 as sp
+from benchmark_spmv_using_csr_gb300 import gen
+
+pytestmark = pytest.mark.gpu
+
+
+def _pinned(a: np.ndarray) -> torch.Tensor:
+    return torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+
+
+@pytest.mark.parametrize("vt", [sp.VALUE_F64, sp.VALUE_F32])
+@pytest.mark.parametrize("count", [1, 2, 5])
+def test_stream_matches_per_call(cuda_ok, vt, count):
+    a = gen.powerlaw(40000, seed=21)
+    dt = sp.host_dtype(vt)
+    xs = [_pinned(gen.uniform_int(a.n, 30 + i, 10).astype(dt)) for i in range(count)]
+    ys = [_pinned(np.full(a.m, -1, dt)) for _ in range(count)]
+    val = gen.uniform_int(a.nnz, 7, 10).astype(dt)
+    h = sp.BhsparseSpmvCuda(vt)
+    y0 = np.zeros(a.m, dt)
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, val, xs[0].numpy(), y0) == 0
+    assert h.run_stream([x.data_ptr() for x in xs], [y.data_ptr() for y in ys]) == 0, h.last_error
+    for i in range(count):  # integer data: exact against the serial loop
+        yr = oracle.csr_serial(a.row_ptr, a.col, val.astype(np.float64),
+                               xs[i].numpy().astype(np.float64))
+        assert np.array_equal(ys[i].numpy().astype(np.float64), yr), i
+    # the per-call path on the same handle still works afterwards
+    assert h.set_x(xs[-1].numpy()) == 0 and h.run_benchmark() == 0 and h.get_y() == 0
+    assert np.array_equal(y0, ys[-1].numpy())
+    h.close()
+
+
+def test_stream_real_values_and_reuse(cuda_ok):
+    a = gen.stencil3d(40, 30, 20, seed=4)
+    xs = [_pinned(gen.uniform(a.n, 50 + i)) for i in range(6)]
+    ys = [_pinned(np.zeros(a.m)) for _ in range(6)]
+    h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, xs[0].numpy(),
+                         np.zeros(a.m)) == 0
+    for _ in range(2):  # a second stream call reuses the buffers and streams
+        assert h.run_stream([x.data_ptr() for x in xs], [y.data_ptr() for y in ys]) == 0
+        for x, y in zip(xs, ys):
+            ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x.numpy())
+            scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, x.numpy())
+            assert oracle.componentwise_error(y.numpy(), ystar, scale) <= TOL_F64
+    assert h.run_stream([], []) == 0
+    h.close()
+
+
+def test_stream_rejects_mixed_and_nulls(cuda_ok):
+    a = gen.stencil2d(20, 20)
+    h = sp.BhsparseSpmvCuda(sp.VALUE_MIXED_F32)
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, np.ones(a.n),
+                         np.zeros(a.m)) == 0
+    x = _pinned(np.ones(a.n))
+    y = _pinned(np.zeros(a.m))
+    assert h.run_stream([x.data_ptr()], [y.data_ptr()]) == sp.BHSPARSE_INVALID_ARGUMENT
+    h.close()
+    h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, np.ones(a.n),
+                         np.zeros(a.m)) == 0
+    assert h.run_stream([0], [y.data_ptr()]) == sp.BHSPARSE_INVALID_ARGUMENT
+    h.close()
