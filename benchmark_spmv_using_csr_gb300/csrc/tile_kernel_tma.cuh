@@ -19,6 +19,8 @@
 #pragma once
 #include <cuda.h>
 
+#include <atomic>
+
 #include "tile_kernel.cuh"
 
 namespace spmv {
@@ -373,16 +375,17 @@ cudaError_t launch_tiles_tma_t(const TileArgs<P>& a, int tpw, int nworkers, int 
             return launch_tiles<P>(a, c, st);
         }
         // the shared-memory opt-in is a per-device function attribute: set it once per device
-        static unsigned long long attr_set = 0ull;
+        // (setting it twice from racing host threads is harmless; the flag word is atomic)
+        static std::atomic<unsigned long long> attr_set{0ull};
         int dev = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess) return e;
         const unsigned long long bit = 1ull << (dev & 63);
-        if (!(attr_set & bit)) {
+        if (!(attr_set.load(std::memory_order_acquire) & bit)) {
             e = cudaFuncSetAttribute(k_tiles_tma<P, S, WARPS, NSTAGE>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
             if (e != cudaSuccess) return e;
-            attr_set |= bit;
+            attr_set.fetch_or(bit, std::memory_order_release);
         }
         const int blocks = (nworkers + WARPS - 1) / WARPS;
         k_tiles_tma<P, S, WARPS, NSTAGE>
