@@ -18,8 +18,8 @@ Metric: SpMV HBM GB/s on the algorithmic bytes B = nnz*(s_val+4) + (m+1)*4 + n*s
   pinned host memory and its y downloaded inside the timed region: bhsp_run_stream over the
   K steps (copies of neighbouring steps overlap each SpMV); ``e2e.per_call`` is the
   reference's per-call sequence bhsp_set_x / bhsp_run_benchmark / bhsp_get_y.
-* ``roofline``: the tile kernel alone (CUDA events between its launch and the
-  calibration launch) against the measured HBM copy bandwidth.
+* ``roofline``: the tile kernel alone (launched on its own between CUDA events, L2 flushed
+  before each) against the measured HBM copy bandwidth.
 * ``cpu_baseline``: the reference's serial CSR loop (spmv_cuda/main.cu:755-761, a port in
   oracle/) on one host core over whole-matrix passes.
 * ``--impl reference``: the reference's OpenMP CSR loop (spmv_cuda/main.cu:377-393, same
@@ -288,29 +288,43 @@ def run_ours(args) -> None:
                 step_async()
             stream.synchronize()
 
-    # timed region: exactly K steps, L2 flushed before each, events around both phases
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    # timed region: exactly K steps (tile kernel + calibration, the calibration launched as a
+    # programmatic dependent), L2 flushed before each, CUDA events around each step
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
     barrier()
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
         for i in range(args.steps):
             flush.fill_(i & 0xFF)
-            e0, e1, e2 = ev[i]
+            e0, e1 = ev[i]
+            e0.record(stream)
+            assert h.run_phase(sptr, 3) == 0, h.last_error
+            e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    assert h.check() == 0, h.last_error
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    total_s = max_over_ranks(sum(step_ms) / 1e3, dist)
+    value = whole_job_gbs(world, B, args.steps, total_s)
+
+    # the tile kernel alone (roofline) and the calibration alone, each launched on its own
+    # between events, on the same flushed-L2 footing (outside the timed region)
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True)) for _ in range(min(args.steps, 50))]
+    with torch.cuda.stream(stream):
+        for i, (e0, e1, e2) in enumerate(kev):
+            flush.fill_(i & 0xFF)
             e0.record(stream)
             assert h.run_phase(sptr, 1) == 0, h.last_error
             e1.record(stream)
             assert h.run_phase(sptr, 2) == 0, h.last_error
             e2.record(stream)
     torch.cuda.synchronize()
-    barrier()
-    clocks = sampler.stop()
     assert h.check() == 0, h.last_error
-    step_ms = [e0.elapsed_time(e2) for e0, _, e2 in ev]
-    kern_ms = [e0.elapsed_time(e1) for e0, e1, _ in ev]
-    cal_ms = [e1.elapsed_time(e2) for _, e1, e2 in ev]
-    total_s = max_over_ranks(sum(step_ms) / 1e3, dist)
-    value = whole_job_gbs(world, B, args.steps, total_s)
+    kern_ms = [e0.elapsed_time(e1) for e0, e1, _ in kev]
+    cal_ms = [e1.elapsed_time(e2) for _, e1, e2 in kev]
 
     # end to end through the C ABI with host buffers (pinned), copies inside the timed region:
     # (1) bhsp_run_stream over the K steps' right-hand sides (two pinned x and y buffers used
@@ -368,7 +382,10 @@ def run_ours(args) -> None:
             "pct_peak": round(100.0 * value / peak, 2),
             "rel_error": {"componentwise_vs_fp64_dot2": rel_err, "tolerance": 1e-12},
             "phases_ms": {"tile_kernel": round(kmean, 5),
-                          "calibration": round(statistics.mean(cal_ms), 5)},
+                          "calibration_alone": round(statistics.mean(cal_ms), 5),
+                          "note": "each phase launched alone between events; in the timed "
+                                  "steps the calibration is a programmatic dependent of the "
+                                  "tile kernel"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic, "peak_kind": f"{peak_kind} (hbm_gbs copy, burst)",

@@ -385,6 +385,8 @@ __global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
     k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
     __shared__ uint32_t s_words[WARPS][32];
     __shared__ int s_rowof[WARPS][32 * S];
+    // the calibration kernel may be scheduled now; it waits for this grid's completion itself
+    asm volatile("griddepcontrol.launch_dependents;");
     const int warp = threadIdx.x >> 5;
     const int worker = blockIdx.x * WARPS + warp;
     if (worker >= nworkers) return;
@@ -415,31 +417,101 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
-// Carry records -> y, in worker order (deterministic): the first record of each run of equal
-// rows sums the run and adds it to the owner's value.  Also zeroes the leading empty rows,
-// which lie in no tile span (the reference never writes them).
+// Exchange of any carry-record type between lanes (as 32-bit words).
+template <class R>
+__device__ __forceinline__ R rec_shfl_xor(const R& v, int d) {
+    static_assert(sizeof(R) % 4 == 0, "records are whole 32-bit words");
+    constexpr int W = (int)(sizeof(R) / 4);
+    uint32_t w[W];
+    memcpy(w, &v, sizeof(R));
+#pragma unroll
+    for (int i = 0; i < W; ++i) w[i] = __shfl_xor_sync(SPMV_FULL_MASK, w[i], d);
+    R r;
+    memcpy(&r, w, sizeof(R));
+    return r;
+}
+
+// Carry records -> y.  One warp per 32 consecutive records.  A record whose row has no other
+// record (the common case) is added by its own lane.  A row with several records (a row that
+// spans several workers) forms a contiguous run; the warp that holds the run's first record sums
+// it cooperatively: lanes take records 32 apart, then a butterfly reduction, so a run of L
+// records costs ceil(L/32) rounds instead of L dependent loads, in an order fixed by L alone
+// (deterministic).  Also zeroes the leading empty rows, which lie in no tile span (the
+// reference never writes them).
 template <class P>
 __global__ void k_calibrate(const int* __restrict__ rec_row,
                             const typename P::Rec* __restrict__ rec_val, int nworkers,
                             typename P::YT* __restrict__ y, const uint32_t* __restrict__ tile_ptr,
                             int m, uint32_t* err) {
     using Rec = typename P::Rec;
+    using YT = typename P::YT;
+    // launched as a programmatic dependent of the tile kernel: wait until that grid has
+    // completed and its records and y are visible (returns at once for an ordinary launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    for (int base = gw * 32; base < nworkers; base += nwarps * 32) {  // warp-uniform
+        const int w = base + lane;
+        const int r = w < nworkers ? rec_row[w] : -1;
+        const int rprev = (w > 0 && w < nworkers) ? rec_row[w - 1] : -1;
+        const int rnext = w + 1 < nworkers ? rec_row[w + 1] : -1;
+        const bool head = r >= 0 && rprev != r;
+        const bool single = head && rnext != r;
+        if (single) {
+            if (r < m)
+                y[r] = P::out_rec(P::rec_add(P::rec_of_y(y[r]), rec_val[w]));
+            else
+                atomicOr(err, ERR_BAD_TILE);
+        }
+        unsigned runs = __ballot_sync(SPMV_FULL_MASK, head && !single);
+        while (runs) {
+            const int src = __ffs(runs) - 1;
+            runs &= runs - 1;
+            const int w0 = base + src;
+            const int row = __shfl_sync(SPMV_FULL_MASK, r, src);
+            Rec acc = P::rec_of_y(YT(0));
+            for (int v = w0 + lane;; v += 32) {
+                const bool in = v < nworkers && rec_row[v] == row;
+                if (in) acc = P::rec_add(acc, rec_val[v]);
+                if (__ballot_sync(SPMV_FULL_MASK, in) != SPMV_FULL_MASK) break;  // the run ended
+            }
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) acc = P::rec_add(acc, rec_shfl_xor(acc, d));
+            if (lane == 0) {
+                if (row < m)
+                    y[row] = P::out_rec(P::rec_add(P::rec_of_y(y[row]), acc));
+                else
+                    atomicOr(err, ERR_BAD_TILE);
+            }
+        }
+    }
     const int stride = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    for (int w = tid; w < nworkers; w += stride) {
-        const int r = rec_row[w];
-        if (r < 0) continue;
-        if (w > 0 && rec_row[w - 1] == r) continue;
-        Rec s = rec_val[w];
-        for (int v = w + 1; v < nworkers && rec_row[v] == r; ++v) s = P::rec_add(s, rec_val[v]);
-        if (r >= m) {
-            atomicOr(err, ERR_BAD_TILE);
-            continue;
-        }
-        y[r] = P::out_rec(P::rec_add(P::rec_of_y(y[r]), s));
-    }
     const int lead = min((int)(tile_ptr[0] & ROW_MASK), m);
-    for (int r = tid; r < lead; r += stride) y[r] = typename P::YT(0);
+    for (int r = tid; r < lead; r += stride) y[r] = YT(0);
+}
+
+// The calibration launch, as a programmatic dependent of the tile kernel launched just before
+// on the same stream: it is scheduled while the tile kernel drains and waits for it on the
+// device (griddepcontrol.wait), which hides the launch gap between the two.
+template <class P>
+cudaError_t launch_calibrate(const TileArgs<P>& a, int nworkers, cudaStream_t st) {
+    int cb = (nworkers + 255) / 256;
+    if (cb < 1) cb = 1;
+    if (cb > 152 * 8) cb = 152 * 8;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cb);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = (a.phase & 1) ? 1 : 0;  // a dependent only when the tile kernel precedes it
+    return cudaLaunchKernelEx(&cfg, k_calibrate<P>, a.rec_row, a.rec_val, nworkers, a.y,
+                              a.tile_ptr, a.m, a.err);
 }
 
 template <class P, int S, int WARPS>
@@ -450,11 +522,8 @@ cudaError_t launch_tiles_t(const TileArgs<P>& a, int tpw, int nworkers, int ntil
         k_tiles<P, S, WARPS><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
     }
     if (a.phase & 2) {
-        int cb = (nworkers + 255) / 256;
-        if (cb < 1) cb = 1;
-        if (cb > 152 * 8) cb = 152 * 8;
-        k_calibrate<P><<<cb, 256, 0, st>>>(a.rec_row, a.rec_val, nworkers, a.y, a.tile_ptr, a.m,
-                                           a.err);
+        const cudaError_t e = launch_calibrate(a, nworkers, st);
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }

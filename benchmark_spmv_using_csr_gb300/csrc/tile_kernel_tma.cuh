@@ -392,11 +392,8 @@ cudaError_t launch_tiles_tma_t(const TileArgs<P>& a, int tpw, int nworkers, int 
             <<<blocks, WARPS * 32, bytes, st>>>(a, maps, tpw, nworkers, ntiles);
     }
     if (a.phase & 2) {
-        int cb = (nworkers + 255) / 256;
-        if (cb < 1) cb = 1;
-        if (cb > 152 * 8) cb = 152 * 8;
-        k_calibrate<P><<<cb, 256, 0, st>>>(a.rec_row, a.rec_val, nworkers, a.y, a.tile_ptr, a.m,
-                                           a.err);
+        const cudaError_t e = launch_calibrate(a, nworkers, st);
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }
