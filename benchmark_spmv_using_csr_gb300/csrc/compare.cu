@@ -23,11 +23,11 @@ __global__ void __launch_bounds__(256) k_csr_vector(int m, const int* __restrict
                                                     const VT* __restrict__ val,
                                                     const VT* __restrict__ x, VT* __restrict__ y) {
     const int lane = threadIdx.x & (TPV - 1);
-    const int vec = (blockIdx.x * blockDim.x + threadIdx.x) / TPV;
-    const int nvec = gridDim.x * blockDim.x / TPV;
+    const long long vec = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / TPV;
+    const long long nvec = (long long)gridDim.x * blockDim.x / TPV;  // 64-bit: m may be near 2^31
     const unsigned mask = TPV == 32 ? 0xffffffffu
                                     : (((1u << TPV) - 1u) << ((threadIdx.x & 31) & ~(TPV - 1)));
-    for (int row = vec; row < m; row += nvec) {
+    for (long long row = vec; row < m; row += nvec) {
         const int rs = __ldg(row_ptr + row);
         const int re = __ldg(row_ptr + row + 1);
         VT sum = VT(0);

@@ -25,7 +25,8 @@ __global__ void k_tile_rows(const int* __restrict__ row_ptr, int m, int nnz, int
 // result does not depend on the order of the atomics.
 __global__ void k_mark_dirty(const int* __restrict__ row_ptr, int m, int tile, int ntiles,
                              uint32_t* __restrict__ tile_ptr) {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+    const long long stride = (long long)gridDim.x * blockDim.x;  // 64-bit: m may be near 2^31
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < m; r += stride) {
         const int o = __ldg(row_ptr + r);
         if (o != __ldg(row_ptr + r + 1)) continue;
         int t = (o % tile == 0) ? o / tile - 1 : o / tile;
@@ -57,12 +58,13 @@ __global__ void k_bitflags(const int* __restrict__ row_ptr, int m, int nnz, int 
 // Any violation sets a bit in *bad (bit0 row_ptr, bit1 col_idx).
 __global__ void k_validate(const int* __restrict__ row_ptr, const int* __restrict__ col, int m,
                            int n, int nnz, uint32_t* bad) {
-    const int stride = gridDim.x * blockDim.x;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    // 64-bit counters: m and nnz may be within one stride of 2^31
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (tid == 0 && (row_ptr[0] != 0 || row_ptr[m] != nnz)) atomicOr(bad, 1u);
-    for (int r = tid; r < m; r += stride)
+    for (long long r = tid; r < m; r += stride)
         if (__ldg(row_ptr + r) > __ldg(row_ptr + r + 1)) atomicOr(bad, 1u);
-    for (int e = tid; e < nnz; e += stride) {
+    for (long long e = tid; e < nnz; e += stride) {
         const int c = __ldg(col + e);
         if (c < 0 || c >= n) atomicOr(bad, 2u);
     }

@@ -486,10 +486,10 @@ __global__ void k_calibrate(const int* __restrict__ rec_row,
             }
         }
     }
-    const int stride = gridDim.x * blockDim.x;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const int lead = min((int)(tile_ptr[0] & ROW_MASK), m);
-    for (int r = tid; r < lead; r += stride) y[r] = YT(0);
+    for (long long r = tid; r < lead; r += stride) y[r] = YT(0);
 }
 
 // The calibration launch, as a programmatic dependent of the tile kernel launched just before

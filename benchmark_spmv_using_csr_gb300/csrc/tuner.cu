@@ -98,7 +98,8 @@ __global__ void k_row_features(const int* __restrict__ row_ptr, int m,
     __syncthreads();
     unsigned long long sum = 0, sq = 0, mx = 0, empty = 0;
     unsigned long long bins[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+    const long long stride = (long long)gridDim.x * blockDim.x;  // 64-bit: m may be near 2^31
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < m; r += stride) {
         const unsigned long long L = (unsigned long long)(__ldg(row_ptr + r + 1) - __ldg(row_ptr + r));
         sum += L;
         sq += L * L;
