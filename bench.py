@@ -43,6 +43,8 @@ METRIC = "SpMV HBM GB/s (% of peak), mixed/batched vs plain FP64 at stated rel. 
 UNIT = "GB/s"
 FALLBACK_HBM_GBS = 6800.0
 FLUSH_BYTES = 256 << 20
+# fully random 8-byte gathers into a 33.5 MB L2-resident vector, all SMs, measured on GB300
+GATHER_PEAK_G = 289.0
 
 WORKLOAD_TEXT = {
     "powerlaw_4m": "power-law m=n=4,194,304: row lengths floor(1.98*U^(-1/1.1)) clipped to "
@@ -386,6 +388,12 @@ def run_ours(args) -> None:
                           "note": "each phase launched alone between events; in the timed "
                                   "steps the calibration is a programmatic dependent of the "
                                   "tile kernel"},
+            "gather_roofline": None if args.workload != "powerlaw_4m" else {
+                "unit": "G gathers/s", "achieved": round(a.nnz / (kmean * 1e-3) / 1e9, 1),
+                "peak": GATHER_PEAK_G, "frac": round(a.nnz / (kmean * 1e-3) / 1e9 / GATHER_PEAK_G, 3),
+                "note": "random 8-byte x gathers (one per non-zero) against the rate a probe of "
+                        "fully random gathers into an L2-resident vector reaches on GB300 "
+                        "(~1 distinct line per clock per SM); the binding unit on this matrix"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic, "peak_kind": f"{peak_kind} (hbm_gbs copy, burst)",
@@ -408,6 +416,8 @@ def run_ours(args) -> None:
     if rank == 0 and args.forms:
         line["forms"] = measure_forms(args, a, x, ystar)
         line["comparators"] = measure_comparators(args, a, x, ystar)
+    if rank == 0 and args.forms:
+        line["other_configs"] = measure_other_configs(args)
     if rank == 0 and args.batched:
         line["batched"] = measure_batched(args)
     if rank == 0 and args.cpu_baseline > 0:
@@ -459,6 +469,69 @@ def measure_forms(args, a, x, ystar) -> dict:
             "gnnz_per_s": round(a.nnz / (ms * 1e-3) / 1e9, 2),
             "normwise_err_vs_fp64_oracle": oracle.normwise_error(y, ystar)}
         h.close()
+    return out
+
+
+def measure_fp64(args, a, x, config=None) -> dict:
+    """Plain FP64 through the handle on one matrix: device GB/s per whole step (L2 flushed
+    before each, CUDA events), the schedule (autotuned unless given), and the componentwise
+    error against the FP64 compensated oracle."""
+    import numpy as np
+    import torch
+
+    import benchmark_spmv_using_csr_gb300 as sp
+    import oracle
+    tuning = autotune_workload(a, x) if config is None else None
+    cfg = tuning["pick"] if tuning else config
+    h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    assert h.set_config(*cfg) == 0, h.last_error
+    y = np.zeros(max(a.m, 1))
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x, y) == 0, h.last_error
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    steps = max(10, min(args.steps, 50))
+    with torch.cuda.stream(stream):
+        for _ in range(5):
+            assert h.run_phase(sptr, 3) == 0, h.last_error
+        evs = []
+        for i in range(steps):
+            flush.fill_(i & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            assert h.run_phase(sptr, 3) == 0, h.last_error
+            e1.record(stream)
+            evs.append((e0, e1))
+    torch.cuda.synchronize()
+    assert h.check() == 0 and h.get_y() == 0, h.last_error
+    ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in evs)
+    B = alg_bytes(a.m, a.n, a.nnz, 8, 8, 8)
+    err = oracle.componentwise_error(y[:a.m], oracle.csr_dot2(a.row_ptr, a.col, a.val, x),
+                                     oracle.csr_absrow(a.row_ptr, a.col, a.val, x))
+    h.close()
+    return {"gbs": round(B / (ms * 1e-3) / 1e9, 1), "ms_per_step": round(ms, 5),
+            "pct_of_peak": round(100 * B / (ms * 1e-3) / 1e9 / measured_peak()[0], 1),
+            "bytes_per_step": B, "schedule": list(cfg),
+            "componentwise_err_vs_fp64_oracle": err, "tolerance": 1e-12}
+
+
+def measure_other_configs(args) -> dict:
+    """The benchmark's other matrices: the 27-point stencil (plain FP64 and the FP32- and
+    BF16-stored forms with their errors) and the 5-point Laplacian (plain FP64; the case the
+    reference runs on the CPU, with the serial loop's rate beside it)."""
+    import oracle
+    out = {}
+    a, x = make_workload("stencil27_160")
+    ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)
+    out["stencil27_160"] = {"m": a.m, "nnz": a.nnz, "fp64": measure_fp64(args, a, x),
+                            "forms": measure_forms(args, a, x, ystar)}
+    del a, x, ystar
+    a, x = make_workload("stencil5_256")
+    B = alg_bytes(a.m, a.n, a.nnz, 8, 8, 8)
+    r = measure_fp64(args, a, x)
+    r["note"] = "5.2 MB of bytes: L2-resident after the flush write and launch-bound"
+    out["stencil5_256"] = {"m": a.m, "nnz": a.nnz, "fp64": r,
+                           "cpu_serial": cpu_baseline(a, x, B, 1.0)}
     return out
 
 
@@ -534,8 +607,8 @@ def cpu_openmp(a, x, B, seconds: float) -> dict:
 
 
 def autotune_workload(a, x) -> dict:
-    """Run the library's autotuner (every candidate schedule, median of 5 timed runs) on the
-    workload and return its table and pick."""
+    """Run the library's autotuner (every candidate schedule, median of 11 timed runs, L2
+    flushed before each) on the workload and return its table and pick."""
     import torch
 
     import benchmark_spmv_using_csr_gb300 as sp
@@ -543,7 +616,7 @@ def autotune_workload(a, x) -> dict:
     rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
     val, xd = torch.from_numpy(a.val).cuda(), torch.from_numpy(x).cuda()
     y = torch.zeros(a.m, dtype=torch.float64, device="cuda")
-    ms, best = tune.autotune(sp.VALUE_F64, rp, ci, val, xd, y, warmup=2, reps=5)
+    ms, best = tune.autotune(sp.VALUE_F64, rp, ci, val, xd, y, warmup=2, reps=11)
     cands = tune.candidates()
     del rp, ci, val, xd, y
     torch.cuda.empty_cache()

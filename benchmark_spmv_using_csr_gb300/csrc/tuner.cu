@@ -18,11 +18,11 @@ namespace {
 struct Cand {
     int seg, tpw, warps;
 };
-// S in {8,16,32} x tiles-per-worker in {1,4,16} x warps-per-CTA in {4,8}; direct loads.
+// S in {8,16,32} x tiles-per-worker in {1,4,8,16} x warps-per-CTA in {4,8}; direct loads.
 const Cand kCands[] = {
-    {8, 1, 4},  {8, 1, 8},  {8, 4, 4},  {8, 4, 8},  {8, 16, 4},  {8, 16, 8},
-    {16, 1, 4}, {16, 1, 8}, {16, 4, 4}, {16, 4, 8}, {16, 16, 4}, {16, 16, 8},
-    {32, 1, 4}, {32, 1, 8}, {32, 4, 4}, {32, 4, 8}, {32, 16, 4}, {32, 16, 8},
+    {8, 1, 4},  {8, 1, 8},  {8, 4, 4},  {8, 4, 8},  {8, 8, 4},  {8, 8, 8},  {8, 16, 4},  {8, 16, 8},
+    {16, 1, 4}, {16, 1, 8}, {16, 4, 4}, {16, 4, 8}, {16, 8, 4}, {16, 8, 8}, {16, 16, 4}, {16, 16, 8},
+    {32, 1, 4}, {32, 1, 8}, {32, 4, 4}, {32, 4, 8}, {32, 8, 4}, {32, 8, 8}, {32, 16, 4}, {32, 16, 8},
 };
 constexpr int kNumCands = sizeof(kCands) / sizeof(kCands[0]);
 
@@ -52,6 +52,21 @@ extern "C" int bhsp_autotune(int value_type, int m, int n, int nnz, const int* d
         if (e0) cudaEventDestroy(e0);
         return BHSPARSE_CUDA_ERROR;
     }
+    // a scratch buffer of twice the L2 size, written before every timed run so that each run
+    // starts with the matrix and x out of L2 (skipped if it cannot be allocated)
+    void* flush = nullptr;
+    size_t flush_bytes = 0;
+    {
+        int dev = 0, l2 = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) == cudaSuccess && l2 > 0) {
+            flush_bytes = 2 * (size_t)l2;
+            if (cudaMalloc(&flush, flush_bytes) != cudaSuccess) {
+                flush = nullptr;
+                cudaGetLastError();  // clear the failed allocation
+            }
+        }
+    }
     int best_i = -1;
     float best_ms = 0.f;
     std::vector<float> t((size_t)reps);
@@ -62,7 +77,9 @@ extern "C" int bhsp_autotune(int value_type, int m, int n, int nnz, const int* d
         if (rc) break;
         for (int w = 0; w < warmup && rc == 0; ++w) rc = bhsp_plan_execute(p, d_val, d_x, d_y, stream);
         for (int r = 0; r < reps && rc == 0; ++r) {
-            if (cudaEventRecord(e0, st) != cudaSuccess) rc = BHSPARSE_CUDA_ERROR;
+            if (flush && cudaMemsetAsync(flush, r & 0xff, flush_bytes, st) != cudaSuccess)
+                rc = BHSPARSE_CUDA_ERROR;
+            if (!rc && cudaEventRecord(e0, st) != cudaSuccess) rc = BHSPARSE_CUDA_ERROR;
             if (!rc) rc = bhsp_plan_execute(p, d_val, d_x, d_y, stream);
             if (!rc && cudaEventRecord(e1, st) != cudaSuccess) rc = BHSPARSE_CUDA_ERROR;
             if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = BHSPARSE_CUDA_ERROR;
@@ -80,6 +97,7 @@ extern "C" int bhsp_autotune(int value_type, int m, int n, int nnz, const int* d
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (flush) cudaFree(flush);
     if (best) *best = best_i;
     return rc;
 }

@@ -129,8 +129,14 @@ class MLP:
 class LearnedTuner:
     """Features -> schedule, trained on autotuner timing tables; falls back to the sweep."""
 
-    def __init__(self, n_out: int | None = None, hidden: int = HIDDEN, seed: int = 0):
-        self.n_out = len(tune.candidates()) if n_out is None else n_out
+    def __init__(self, n_out: int | None = None, hidden: int = HIDDEN, seed: int = 0,
+                 candidates=None):
+        # the schedules the network's outputs stand for (the timing table's columns)
+        self.candidates = [tuple(int(v) for v in c) for c in
+                           (tune.candidates() if candidates is None else candidates)]
+        self.n_out = len(self.candidates) if n_out is None else n_out
+        if self.n_out != len(self.candidates):
+            raise ValueError("one network output per candidate schedule")
         self.net = MLP(tune.NUM_FEATURES, hidden, self.n_out, seed=seed)
         self.threshold = 0.0
 
@@ -202,19 +208,21 @@ class LearnedTuner:
         pick, conf = self.predict(f)
         if conf[0] >= self.threshold:
             return {"index": int(pick[0]), "confidence": float(conf[0]), "fallback": False,
-                    "config": tune.candidates()[int(pick[0])]}
+                    "config": self.candidates[int(pick[0])]}
         ms, best = tune.autotune(value_type, row_ptr, col_idx, val, x, y, n=n)
         return {"index": best, "confidence": float(conf[0]), "fallback": True,
                 "config": tune.candidates()[best], "ms": ms}
 
     def save(self, path: str) -> None:
         np.savez(path, params=self.net.get_params(), mean=self.net.mean, std=self.net.std,
-                 threshold=np.float32(self.threshold), n_out=self.n_out, hidden=self.net.hidden)
+                 threshold=np.float32(self.threshold), n_out=self.n_out, hidden=self.net.hidden,
+                 candidates=np.array(self.candidates, np.int32))
 
     @classmethod
     def load(cls, path: str) -> "LearnedTuner":
         d = np.load(path)
-        t = cls(n_out=int(d["n_out"]), hidden=int(d["hidden"]))
+        cands = d["candidates"] if "candidates" in d.files else None
+        t = cls(n_out=int(d["n_out"]), hidden=int(d["hidden"]), candidates=cands)
         t.net.set_params(d["params"])
         t.net.set_normalization(d["mean"], d["std"])
         t.threshold = float(d["threshold"])

@@ -27,10 +27,11 @@ def main(data_path: str, out_prefix: str) -> dict:
     # the confidence threshold is calibrated on matrices the network was not fitted on: fit on
     # 85 % of the training set, calibrate on the other 15 %, then refit on all of it
     nfit = int(0.85 * ntr)
-    probe = mlp.LearnedTuner(n_out=ms.shape[1], seed=0)
+    cands = d["candidates"] if "candidates" in d.files else None
+    probe = mlp.LearnedTuner(n_out=ms.shape[1], seed=0, candidates=cands)
     probe.fit(ftr[:nfit], mtr[:nfit], epochs=EPOCHS, batch=256, lr=LR, weight_decay=WD)
     threshold = probe.calibrate_threshold(ftr[nfit:], mtr[nfit:], target=0.97, max_fallback=0.25)
-    tuner = mlp.LearnedTuner(n_out=ms.shape[1], seed=0)
+    tuner = mlp.LearnedTuner(n_out=ms.shape[1], seed=0, candidates=cands)
     hist = tuner.fit(ftr, mtr, epochs=EPOCHS, batch=256, lr=LR, weight_decay=WD)
     tuner.threshold = threshold
     ev_te = tuner.evaluate(fte, mte)

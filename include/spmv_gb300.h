@@ -196,8 +196,10 @@ int bhsp_tune_num_candidates(void);
 int bhsp_tune_candidate(int index, int* seg, int* tiles_per_worker, int* warps_per_cta,
                         int* stages);
 /* Autotuner: validates the CSR, then times y = A.x for every candidate on the given device
- * buffers (`warmup` untimed runs, then the median of `reps` CUDA-event-timed runs) and writes
- * ms_out[bhsp_tune_num_candidates()] and the index of the fastest to *best.  Synchronous. */
+ * buffers (`warmup` untimed runs, then the median of `reps` CUDA-event-timed runs, each
+ * preceded by a write of twice the L2 size so that it starts with the matrix and x out of L2)
+ * and writes ms_out[bhsp_tune_num_candidates()] and the index of the fastest to *best.
+ * Synchronous. */
 int bhsp_autotune(int value_type, int m, int n, int nnz, const int* d_row_ptr,
                   const int* d_col_idx, const void* d_val, const void* d_x, void* d_y, int warmup,
                   int reps, float* ms_out, int* best, void* stream);

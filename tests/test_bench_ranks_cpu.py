@@ -33,7 +33,7 @@ def _rank_main(rank, world, port, out):
 
 def test_max_over_ranks_gloo_world2():
     world = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()  # no fork of this multi-threaded process
     mp.spawn(_rank_main, args=(world, _free_port(), out), nprocs=world, join=True)
     for r in range(world):
         t, gbs = out[r]

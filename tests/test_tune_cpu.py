@@ -6,7 +6,7 @@ from benchmark_spmv_using_csr_gb300 import gen, tune
 
 def test_candidate_table():
     c = tune.candidates()
-    assert len(c) == 18
+    assert len(c) == 24
     assert len(set(c)) == len(c)
     for seg, tpw, warps, stages in c:
         assert seg in (8, 16, 32) and tpw >= 1 and warps in (4, 8) and stages == 0
@@ -38,8 +38,9 @@ def test_tune_cache_roundtrip(tmp_path):
     p = str(tmp_path / "t.json")
     cache = tune.TuneCache(p)
     f = np.arange(16, dtype=np.float32)
-    cache.put(0, f, np.ones(18, np.float32) * 2, 5)
+    k = len(tune.candidates())
+    cache.put(0, f, np.ones(k, np.float32) * 2, 5)
     cache.save()
     again = tune.TuneCache(p)
     ms, best = again.get(0, f)
-    assert best == 5 and ms.shape == (18,) and again.get(1, f) is None
+    assert best == 5 and ms.shape == (k,) and again.get(1, f) is None
