@@ -131,11 +131,15 @@ class LearnedTuner:
 
     def __init__(self, n_out: int | None = None, hidden: int = HIDDEN, seed: int = 0,
                  candidates=None):
-        # the schedules the network's outputs stand for (the timing table's columns)
-        self.candidates = [tuple(int(v) for v in c) for c in
-                           (tune.candidates() if candidates is None else candidates)]
+        # the schedules the network's outputs stand for (the timing table's columns); a network
+        # with another number of outputs and no list is a plain classifier (no choose())
+        if candidates is None:
+            live = tune.candidates()
+            candidates = live if n_out is None or n_out == len(live) else None
+        self.candidates = (None if candidates is None else
+                           [tuple(int(v) for v in c) for c in candidates])
         self.n_out = len(self.candidates) if n_out is None else n_out
-        if self.n_out != len(self.candidates):
+        if self.candidates is not None and self.n_out != len(self.candidates):
             raise ValueError("one network output per candidate schedule")
         self.net = MLP(tune.NUM_FEATURES, hidden, self.n_out, seed=seed)
         self.threshold = 0.0
@@ -203,6 +207,8 @@ class LearnedTuner:
 
     def choose(self, value_type: int, row_ptr, col_idx, val, x, y, n: int | None = None) -> dict:
         """Pick a schedule for a device matrix: the network if confident, else the sweep."""
+        if self.candidates is None:
+            raise ValueError("this network's outputs are not tied to candidate schedules")
         n = x.numel() if n is None else n
         f = tune.row_features(row_ptr, n)
         pick, conf = self.predict(f)
@@ -216,12 +222,12 @@ class LearnedTuner:
     def save(self, path: str) -> None:
         np.savez(path, params=self.net.get_params(), mean=self.net.mean, std=self.net.std,
                  threshold=np.float32(self.threshold), n_out=self.n_out, hidden=self.net.hidden,
-                 candidates=np.array(self.candidates, np.int32))
+                 candidates=np.array(self.candidates if self.candidates else [], np.int32))
 
     @classmethod
     def load(cls, path: str) -> "LearnedTuner":
         d = np.load(path)
-        cands = d["candidates"] if "candidates" in d.files else None
+        cands = d["candidates"] if "candidates" in d.files and d["candidates"].size else None
         t = cls(n_out=int(d["n_out"]), hidden=int(d["hidden"]), candidates=cands)
         t.net.set_params(d["params"])
         t.net.set_normalization(d["mean"], d["std"])
