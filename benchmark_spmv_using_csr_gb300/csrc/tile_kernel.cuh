@@ -80,8 +80,10 @@ __device__ __forceinline__ float to_compute(__nv_bfloat16 v) { return __bfloat16
 // fewer live registers), 8 otherwise.
 template <int S, typename XT>
 __host__ __device__ constexpr int chunk_width() {
-    // x entries wider than 8 bytes (several right-hand sides) use 4-wide chunks too
-    return (S == 8 || sizeof(XT) > 8) ? 4 : 8;
+    // x entries wider than 8 bytes (several right-hand sides) use 4-wide chunks, and 8 right-
+    // hand sides (32-byte entries) 2-wide ones: 160 instead of 190 registers, 12 instead of 8
+    // resident warps per SM, +19 % on the batched workload at k = 8
+    return sizeof(XT) > 16 ? 2 : (S == 8 || sizeof(XT) > 8) ? 4 : 8;
 }
 
 template <int CW, typename XT>
