@@ -18,6 +18,8 @@ Metric: SpMV HBM GB/s on the algorithmic bytes B = nnz*(s_val+4) + (m+1)*4 + n*s
   pinned host memory and its y downloaded inside the timed region: bhsp_run_stream over the
   K steps (copies of neighbouring steps overlap each SpMV); ``e2e.per_call`` is the
   reference's per-call sequence bhsp_set_x / bhsp_run_benchmark / bhsp_get_y.
+* ``sector_roofline`` (power-law matrix): L2 -> SM sectors per second against the random-gather
+  probe's rate, the unit that binds on that matrix.
 * ``roofline``: the tile kernel alone (launched on its own between CUDA events, L2 flushed
   before each) against the measured HBM copy bandwidth.
 * ``cpu_baseline``: the reference's serial CSR loop (spmv_cuda/main.cu:755-761, a port in
@@ -43,8 +45,15 @@ METRIC = "SpMV HBM GB/s (% of peak), mixed/batched vs plain FP64 at stated rel. 
 UNIT = "GB/s"
 FALLBACK_HBM_GBS = 6800.0
 FLUSH_BYTES = 256 << 20
-# fully random 8-byte gathers into a 33.5 MB L2-resident vector, all SMs, measured on GB300
-GATHER_PEAK_G = 289.0
+# fully random 8-byte gathers into a 33.5 MB L2-resident vector, all SMs, measured on GB300:
+# one 32-byte sector per gather
+SECTOR_PEAK_G = 289.0
+
+
+def l2_sectors(a) -> int:
+    """Algorithmic L2 -> SM sectors of one plain-FP64 SpMV: one per x gather (random columns)
+    plus the val, col_idx and row_ptr streams in 32-byte sectors."""
+    return int(a.nnz + (a.nnz * 12 + (a.m + 1) * 4 + 31) // 32)
 
 WORKLOAD_TEXT = {
     "powerlaw_4m": "power-law m=n=4,194,304: row lengths floor(1.98*U^(-1/1.1)) clipped to "
@@ -388,12 +397,16 @@ def run_ours(args) -> None:
                           "note": "each phase launched alone between events; in the timed "
                                   "steps the calibration is a programmatic dependent of the "
                                   "tile kernel"},
-            "gather_roofline": None if args.workload != "powerlaw_4m" else {
-                "unit": "G gathers/s", "achieved": round(a.nnz / (kmean * 1e-3) / 1e9, 1),
-                "peak": GATHER_PEAK_G, "frac": round(a.nnz / (kmean * 1e-3) / 1e9 / GATHER_PEAK_G, 3),
-                "note": "random 8-byte x gathers (one per non-zero) against the rate a probe of "
-                        "fully random gathers into an L2-resident vector reaches on GB300 "
-                        "(~1 distinct line per clock per SM); the binding unit on this matrix"},
+            "sector_roofline": None if args.workload != "powerlaw_4m" else {
+                "unit": "G sectors/s", "achieved": round(l2_sectors(a) / (kmean * 1e-3) / 1e9, 1),
+                "peak": SECTOR_PEAK_G,
+                "frac": round(l2_sectors(a) / (kmean * 1e-3) / 1e9 / SECTOR_PEAK_G, 3),
+                "sectors_per_launch": l2_sectors(a),
+                "note": "32-byte sectors the SMs take from L2 per SpMV (one per random x gather, "
+                        "plus val / col_idx / row_ptr at 32 bytes a sector) against the sector "
+                        "rate of a probe of fully random gathers into an L2-resident vector on "
+                        "GB300 (~1 sector per clock per SM); the binding unit on this matrix "
+                        "(ncu: l1tex__m_xbar2l1tex_read_sectors runs at this rate)"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic, "peak_kind": f"{peak_kind} (hbm_gbs copy, burst)",
