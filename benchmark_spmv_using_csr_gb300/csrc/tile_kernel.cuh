@@ -101,9 +101,18 @@ __device__ __forceinline__ void store_row(YT* y, int m, int row, YT v, uint32_t*
         atomicOr(err, ERR_BAD_TILE);
 }
 
+// Loops over the lanes of a warp that run once per tile or less: fully unrolled for scalar
+// accumulators, kept rolled for the batched form's wide ones (8 right-hand sides), whose
+// unrolled copies would crowd the multiply-add loop out of the instruction cache.
+template <class P>
+constexpr int cold_unroll() {
+    return sizeof(typename P::Acc) > 16 ? 1 : 5;
+}
+
 template <class P>
 __device__ __forceinline__ typename P::Acc warp_sum_acc(typename P::Acc v) {
-#pragma unroll
+    constexpr int U = cold_unroll<P>();
+#pragma unroll U
     for (int d = 16; d > 0; d >>= 1) v = P::add(v, sh_xor(v, d));
     return v;
 }
@@ -191,7 +200,8 @@ __device__ __forceinline__ typename P::Acc head_run_scan(typename P::Acc head, b
         }
     } else {
         int stop = has ? 1 : 0;
-#pragma unroll
+        constexpr int U = cold_unroll<P>();
+#pragma unroll U
         for (int d = 1; d < 32; d <<= 1) {
             const Acc tv = sh_down(T, d);
             const int sv = __shfl_down_sync(SPMV_FULL_MASK, stop, d);
@@ -306,7 +316,10 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
         if (fmask != 0u && !first_head && lane == 0) run = P::carry_to_acc(carry);
         Acc head = P::zero();
         int cur_row = -1;  // row of this lane's open segment
-#pragma unroll
+        // the chunk loop is unrolled fully, except for wide accumulators (8 right-hand sides):
+        // unrolled by 2 there, to keep the loop in the instruction cache
+        constexpr int UNR = sizeof(Acc) > 16 ? 2 : NC;
+#pragma unroll UNR
         for (int c = 0; c < NC; ++c) {
             // issue: columns of chunk g+2, values and x of chunk g+1
             const int t1 = t + (c + 1) / NC, c1 = (c + 1) % NC;
