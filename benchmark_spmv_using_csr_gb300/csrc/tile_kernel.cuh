@@ -102,11 +102,11 @@ __device__ __forceinline__ void store_row(YT* y, int m, int row, YT v, uint32_t*
 }
 
 // Loops over the lanes of a warp that run once per tile or less: fully unrolled for scalar
-// accumulators, kept rolled for the batched form's wide ones (8 right-hand sides), whose
+// accumulators, kept rolled for the batched form's wide ones (2 or more right-hand sides), whose
 // unrolled copies would crowd the multiply-add loop out of the instruction cache.
 template <class P>
 constexpr int cold_unroll() {
-    return sizeof(typename P::Acc) > 16 ? 1 : 5;
+    return sizeof(typename P::Acc) >= 16 ? 1 : 5;
 }
 
 template <class P>
