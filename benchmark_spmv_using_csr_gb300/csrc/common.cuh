@@ -83,7 +83,8 @@ __device__ __forceinline__ uint64_t policy_evict_last() {
 }
 
 // Cache treatment of the two access streams (compile-time):
-//   1: no L2 policy on either (the val / col stream skips L1 allocation) -- the default: on
+//   1: no L2 policy on either (the val / col stream's whole-sector loads skip L1 allocation) --
+//      the default: on
 //      GB300 it is the fastest on both benchmark matrices (27-point stencil +6 % over 0)
 //   0: val/col stream with an L2 evict-first policy, x gathers with an L2 evict-last policy
 //   2: evict-first on the stream only
@@ -132,11 +133,16 @@ __device__ __forceinline__ void ld_stream_b32x8(const void* p, uint64_t pol, uin
                  : "l"(p), "l"(pol));
 #endif
 }
-// 128-bit streaming load (16-byte aligned)
+// 128-bit and 64-bit stream loads serve chunks narrower than a 32-byte sector: the same lane's
+// next chunk reads the other half (or quarters) of the sector, so these loads allocate in L1
+// and that next read hits there instead of fetching the sector from L2 a second time (column
+// indices at S = 8, FP32 / BF16 values at S = 8, BF16 values at S = 16, the batched form's
+// column indices at 8 right-hand sides).
+// 128-bit stream load (16-byte aligned)
 __device__ __forceinline__ void ld_stream_b32x4(const void* p, uint64_t pol, uint32_t (&v)[4]) {
 #if SPMV_CACHE_MODE == 1
     (void)pol;
-    asm volatile("ld.global.nc.L1::no_allocate.v4.b32 {%0,%1,%2,%3}, [%4];"
+    asm volatile("ld.global.nc.v4.b32 {%0,%1,%2,%3}, [%4];"
                  : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
                  : "l"(p));
 #else
@@ -146,11 +152,11 @@ __device__ __forceinline__ void ld_stream_b32x4(const void* p, uint64_t pol, uin
 #endif
 }
 
-// 64-bit streaming load (8-byte aligned)
+// 64-bit stream load (8-byte aligned)
 __device__ __forceinline__ void ld_stream_b32x2(const void* p, uint64_t pol, uint32_t (&v)[2]) {
 #if SPMV_CACHE_MODE == 1
     (void)pol;
-    asm volatile("ld.global.nc.L1::no_allocate.v2.b32 {%0,%1}, [%2];" : "=r"(v[0]), "=r"(v[1]) : "l"(p));
+    asm volatile("ld.global.nc.v2.b32 {%0,%1}, [%2];" : "=r"(v[0]), "=r"(v[1]) : "l"(p));
 #else
     asm volatile("ld.global.nc.L1::no_allocate" SPMV_STREAM_HINT ".v2.b32 {%0,%1}, [%2], %3;"
                  : "=r"(v[0]), "=r"(v[1])
