@@ -39,7 +39,8 @@ VALUE_MIXED_BF16 = 3
 VALUE_NAMES = {VALUE_F64: "f64", VALUE_F32: "f32", VALUE_MIXED_F32: "mixed_f32",
                VALUE_MIXED_BF16: "mixed_bf16"}
 
-# (non-zeros per lane, tiles per worker, warps per CTA, TMA stages; 0 stages = direct loads)
+# (non-zeros per lane, tiles per worker, warps per CTA, TMA stages; 0 stages = direct loads);
+# BF16 storage defaults to 2 stages (its TMA-staged schedule is the faster one)
 DEFAULT_CONFIG = (16, 8, 4, 0)
 
 

@@ -41,12 +41,17 @@ bool config_ok(const TileConfig& c, int vt) {
     return smem >= 0 && smem <= 227 * 1024;
 }
 
-TileConfig make_config(int seg, int tpw, int warps, int stages) {
+// Default stages: direct loads, except for BF16 storage, whose 16-byte value chunks keep too few
+// bytes in flight for direct loads; its TMA-staged ring is 30 % faster on the 27-point stencil
+// and 6 % on the power-law matrix.
+int default_stages(int vt) { return vt == BHSP_VALUE_MIXED_BF16 ? 2 : kDefaultStages; }
+
+TileConfig make_config(int seg, int tpw, int warps, int stages, int vt) {
     TileConfig c;
     c.seg = seg > 0 ? seg : kDefaultSeg;
     c.tiles_per_worker = tpw > 0 ? tpw : kDefaultTpw;
     c.warps_per_cta = warps > 0 ? warps : kDefaultWarps;
-    c.stages = stages >= 0 ? stages : kDefaultStages;
+    c.stages = stages >= 0 ? stages : default_stages(vt);
     return c;
 }
 
@@ -247,7 +252,7 @@ int spmv::plan_create_impl(bhsp_plan** out, int value_type, int m, int n, int nn
     if (rc) return rc;
     if (!d_row_ptr || (nnz > 0 && !d_col_idx)) return BHSPARSE_INVALID_ARGUMENT;
     if (reinterpret_cast<uintptr_t>(d_col_idx) % 32 != 0) return BHSPARSE_INVALID_ARGUMENT;
-    TileConfig cfg = make_config(seg, tiles_per_worker, warps_per_cta, stages);
+    TileConfig cfg = make_config(seg, tiles_per_worker, warps_per_cta, stages, value_type);
     if (!config_ok(cfg, value_type)) return BHSPARSE_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (validate) {
@@ -364,7 +369,7 @@ struct bhsp_spmv {
     int device = 0;
     bool platform = false;
     bool prepared = false;
-    TileConfig cfg = make_config(0, 0, 0, -1);
+    TileConfig cfg = make_config(0, 0, 0, -1, BHSP_VALUE_F64);  // reset for h->vt in bhsp_create
     int m = 0, n = 0, nnz = 0;
     int* d_row_ptr = nullptr;
     int* d_col = nullptr;
@@ -403,6 +408,7 @@ extern "C" int bhsp_create(bhsp_spmv** out, int value_type) {
     if (!valid_vt(value_type) || !supported_vt(value_type)) return BHSPARSE_UNSUPPORTED_VALUE_TYPE;
     bhsp_spmv* h = new bhsp_spmv;
     h->vt = value_type;
+    h->cfg = make_config(0, 0, 0, -1, value_type);
     *out = h;
     return BHSPARSE_SUCCESS;
 }
@@ -430,7 +436,7 @@ extern "C" int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int 
                                int stages) {
     if (!h) return BHSPARSE_INVALID_ARGUMENT;
     if (h->prepared) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "set_config after prepare_mem");
-    TileConfig c = make_config(seg, tiles_per_worker, warps_per_cta, stages);
+    TileConfig c = make_config(seg, tiles_per_worker, warps_per_cta, stages, h->vt);
     if (!config_ok(c, h->vt)) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "unsupported tile config");
     h->cfg = c;
     return BHSPARSE_SUCCESS;

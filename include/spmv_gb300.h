@@ -86,9 +86,9 @@ int bhsp_set_device(bhsp_spmv* h, int device);
  * warps_per_cta 4 or 8, stages = 0 (each lane streams its values with 256-bit loads) or
  * 2 / 3 / 4 (values and column indices staged in a shared-memory ring of that many tiles by
  * 2D tensor copies; a matrix with no full tile runs the direct-load kernel).  Before
- * prepare_mem; 0 for seg /
- * tiles_per_worker / warps_per_cta and -1 for stages keep the default.  Rejected if the
- * staged ring does not fit in shared memory. */
+ * prepare_mem; 0 for seg / tiles_per_worker / warps_per_cta and -1 for stages keep the default
+ * (16, 8, 4, 0; stages 2 for BHSP_VALUE_MIXED_BF16, whose staged schedule is the faster one).
+ * Rejected if the staged ring does not fit in shared memory. */
 int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int warps_per_cta, int stages);
 int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tiles_per_worker, int* warps_per_cta,
                     int* stages);

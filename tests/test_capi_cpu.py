@@ -58,6 +58,10 @@ def test_config_validation_without_gpu():
     assert s.set_config(8, 1, 6) == sp.BHSPARSE_INVALID_ARGUMENT
     assert s.set_config(8, 1, 4, 1) == sp.BHSPARSE_INVALID_ARGUMENT
     assert s.set_config(16, 4, 8, 3) == sp.BHSPARSE_SUCCESS  # 8 warps x 3 FP64 slots fit
+    b = sp.BhsparseSpmvCuda(sp.VALUE_MIXED_BF16)  # BF16 storage defaults to the staged ring
+    assert b.get_config() == sp.DEFAULT_CONFIG[:3] + (2,)
+    assert b.set_config(8, 0, 0, -1) == sp.BHSPARSE_SUCCESS and b.get_config() == (8, 8, 4, 2)
+    assert b.set_config(16, 8, 4, 0) == sp.BHSPARSE_SUCCESS and b.get_config() == (16, 8, 4, 0)
     # 8 warps x 3 slots of 32 x 32 FP64 runs exceed 227 KB of shared memory
     assert s.set_config(32, 4, 8, 3) == sp.BHSPARSE_INVALID_ARGUMENT
     s.close()
