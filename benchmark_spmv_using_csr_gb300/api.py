@@ -230,6 +230,14 @@ class Plan:
         self._L.bhsp_plan_tiles(self._p, ctypes.byref(tp), ctypes.byref(nt), ctypes.byref(tn))
         return tp.value, nt.value, tn.value
 
+    def chunk_form(self) -> tuple[int, bool]:
+        """(non-empty rows shorter than a chunk, whether the one-head chunk form is on)."""
+        sr, oh = ctypes.c_int(), ctypes.c_int()
+        rc = self._L.bhsp_plan_chunk_form(self._p, ctypes.byref(sr), ctypes.byref(oh))
+        if rc != BHSPARSE_SUCCESS:
+            raise SpmvError(rc, self.last_error)
+        return sr.value, bool(oh.value)
+
     @property
     def last_error(self) -> str:
         return self._L.bhsp_plan_last_error(self._p).decode()

@@ -85,6 +85,8 @@ struct bhsp_plan {
     int* rec_row = nullptr;
     void* rec_val = nullptr;
     uint32_t* err = nullptr;  // device error word
+    int short_rows = 0;     // non-empty rows shorter than one chunk of a lane's slots
+    bool one_head = false;  // the tile kernels take the one-head chunk form
     int device = 0;
     std::string last_error;
 };
@@ -161,6 +163,19 @@ static int plan_build(bhsp_plan* p, cudaStream_t st) {
     PLAN_CUDA(p, cudaMalloc(&p->err, sizeof(uint32_t)));
     PLAN_CUDA(p, cudaMemsetAsync(p->err, 0, sizeof(uint32_t), st));
     PLAN_CUDA(p, launch_partition(p->row_ptr, p->m, p->nnz, tile, p->tile_ptr, st));
+    // the chunk form: rows shorter than the plain / mixed kernels' chunk width (scalar x
+    // entries: 4 slots at S = 8, else 8), counted on the device and read back once
+    const int cw = p->cfg.seg == 8 ? 4 : 8;
+    uint32_t* count = nullptr;
+    uint32_t h = 0;
+    PLAN_CUDA(p, cudaMalloc(&count, sizeof(uint32_t)));
+    cudaError_t e = launch_short_rows(p->row_ptr, p->m, cw, count, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, count, sizeof h, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(count);
+    if (e != cudaSuccess) return cuda_fail(&p->last_error, e, "short-row count");
+    p->short_rows = (int)h;
+    p->one_head = one_head_pays(h, p->nnz, cw);
     return BHSPARSE_SUCCESS;
 }
 
@@ -185,6 +200,7 @@ static int plan_execute(bhsp_plan* p, const void* val, const void* x, void* y, c
             a.n = p->n;
             a.nnz = p->nnz;
             a.phase = phase;
+            a.one_head = p->one_head;
             e = p->vt == BHSP_VALUE_F64 ? launch_plain_f64(a, p->cfg, st) : launch_plain_f32(a, p->cfg, st);
             break;
         }
@@ -204,6 +220,7 @@ static int plan_execute(bhsp_plan* p, const void* val, const void* x, void* y, c
             a.nnz = p->nnz;
             a.bf16 = p->vt == BHSP_VALUE_MIXED_BF16;
             a.phase = phase;
+            a.one_head = p->one_head;
             e = launch_mixed(a, p->cfg, st);
             break;
         }
@@ -313,6 +330,13 @@ extern "C" int bhsp_plan_tiles(const bhsp_plan* p, const uint32_t** d_tile_ptr, 
     if (d_tile_ptr) *d_tile_ptr = p->tile_ptr;
     if (ntiles) *ntiles = p->ntiles;
     if (tile_nnz) *tile_nnz = 32 * p->cfg.seg;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_plan_chunk_form(const bhsp_plan* p, int* short_rows, int* one_head) {
+    if (!p) return BHSPARSE_INVALID_ARGUMENT;
+    if (short_rows) *short_rows = p->short_rows;
+    if (one_head) *one_head = p->one_head ? 1 : 0;
     return BHSPARSE_SUCCESS;
 }
 

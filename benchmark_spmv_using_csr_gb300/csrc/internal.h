@@ -21,6 +21,14 @@ cudaError_t launch_partition(const int* row_ptr, int m, int nnz, int tile, uint3
                              cudaStream_t st);
 cudaError_t launch_bitflags(const int* row_ptr, int m, int nnz, int seg, const uint32_t* tile_ptr,
                             uint32_t* words, cudaStream_t st);
+// *count = non-empty rows shorter than cw non-zeros (zeroed first)
+cudaError_t launch_short_rows(const int* row_ptr, int m, int cw, uint32_t* count, cudaStream_t st);
+// Whether the tile kernels take the one-head chunk form: the short rows can break at most 1/8
+// of the warp-chunks (32 lanes x cw slots).
+inline bool one_head_pays(long long short_rows, long long nnz, int cw) {
+    const long long chunks = (nnz + 32LL * cw - 1) / (32LL * cw);
+    return 8 * short_rows <= chunks;
+}
 cudaError_t launch_validate(const int* row_ptr, const int* col, int m, int n, int nnz,
                             uint32_t* bad, cudaStream_t st);
 
@@ -37,6 +45,7 @@ struct PlainLaunch {
     uint32_t* err;
     int m, n, nnz;
     int phase;  // bit 0: tile kernel, bit 1: calibration kernel
+    bool one_head = false;  // the plan's choice of the one-head chunk form
 };
 cudaError_t launch_plain_f64(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_plain_f32(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
@@ -56,6 +65,7 @@ struct MixedLaunch {
     int m, n, nnz;
     bool bf16;
     int phase;  // bit 0: tile kernel, bit 1: calibration kernel
+    bool one_head = false;  // the plan's choice of the one-head chunk form
 };
 cudaError_t launch_mixed(const MixedLaunch& a, const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_convert_from_f64(const double* src, void* dst, size_t n, bool to_bf16,

@@ -104,6 +104,29 @@ cudaError_t launch_bitflags(const int* row_ptr, int m, int nnz, int seg, const u
     return cudaGetLastError();
 }
 
+// Non-empty rows shorter than cw non-zeros.  Only such a row puts two row heads into one
+// lane's chunk of cw slots (heads at s and s + len share an aligned chunk only if len < cw), and
+// it does so in at most one chunk.
+__global__ void k_short_rows(const int* __restrict__ row_ptr, int m, int cw,
+                             uint32_t* __restrict__ count) {
+    const long long stride = (long long)gridDim.x * blockDim.x;  // 64-bit: m may be near 2^31
+    uint32_t c = 0;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < m; r += stride) {
+        const int len = __ldg(row_ptr + r + 1) - __ldg(row_ptr + r);
+        c += (len > 0 && len < cw) ? 1u : 0u;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(SPMV_FULL_MASK, c, d);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+cudaError_t launch_short_rows(const int* row_ptr, int m, int cw, uint32_t* count, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    if (m > 0) k_short_rows<<<grid_for(m, 256, 152 * 8), 256, 0, st>>>(row_ptr, m, cw, count);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_validate(const int* row_ptr, const int* col, int m, int n, int nnz,
                             uint32_t* bad, cudaStream_t st) {
     long long work = (long long)(m > nnz ? m : nnz);

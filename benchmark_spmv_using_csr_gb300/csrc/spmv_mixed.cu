@@ -69,6 +69,7 @@ cudaError_t launch_mixed(const MixedLaunch& l, const TileConfig& cfg, cudaStream
         a.n = l.n;
         a.nnz = l.nnz;
         a.phase = l.phase;
+        a.one_head = l.one_head;
         return launch_tiles_any(a, cfg, st);
     }
     TileArgs<PolMixed<float>> a;
@@ -85,6 +86,7 @@ cudaError_t launch_mixed(const MixedLaunch& l, const TileConfig& cfg, cudaStream
     a.n = l.n;
     a.nnz = l.nnz;
     a.phase = l.phase;
+    a.one_head = l.one_head;
     return launch_tiles_any(a, cfg, st);
 }
 

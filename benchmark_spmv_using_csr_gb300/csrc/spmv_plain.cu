@@ -68,6 +68,7 @@ static cudaError_t launch_plain_any(const PlainLaunch& l, const TileConfig& cfg,
     a.n = l.n;
     a.nnz = l.nnz;
     a.phase = l.phase;
+    a.one_head = l.one_head;
     return launch_tiles_any<P>(a, cfg, st);
 }
 

@@ -53,6 +53,9 @@ struct TileArgs {
     uint32_t* err;
     int m, n, nnz;
     int phase;  // bit 0: tile kernel, bit 1: calibration kernel
+    // launcher choice, made at plan time: the kernel specialised for the one-head chunk form
+    // (few rows shorter than a chunk, so that most chunks take it)
+    bool one_head = false;
 };
 
 // ---- shuffles for the accumulator types ----
@@ -214,12 +217,62 @@ __device__ __forceinline__ typename P::Acc head_run_scan(typename P::Acc head, b
     return T;
 }
 
+// The segmented multiply-accumulate of one chunk of CW slots of this lane.  cb = the lane's row-
+// head bits for the chunk (its first slot, lane slot kk0, in bit CW-1).  At a head the running
+// sum `run` closes a segment: stored to cur_row when the lane already had a head, else kept as
+// `head` (the slots before the lane's first head); cur_row becomes the head's row.
+//
+// When no lane of the warp has two heads in the chunk (rows of CW non-zeros or more, which the
+// plan's one-head word says is the common case) the slots run branch-free: the head closes the
+// segment by selects and the closed segment is stored once per chunk.  The per-slot branch of
+// the general form runs its body whenever any lane of the warp has a head in that slot, which
+// on such matrices is most slots.
+template <class P, int S, int CW, typename VC, typename XT>
+__device__ __forceinline__ void chunk_segments(bool one_head, uint32_t cb, int kk0,
+                                               const VC (&v)[CW], const XT (&x)[CW],
+                                               typename P::Acc& run, typename P::Acc& head,
+                                               int& cur_row, const int* rowof, int lane,
+                                               const TileArgs<P>& a) {
+    using Acc = typename P::Acc;
+    if (one_head && __all_sync(SPMV_FULL_MASK, (cb & (cb - 1u)) == 0u)) {
+        const int h = cb != 0u ? __clz(cb) - (32 - CW) : CW;  // head slot, CW: none
+        Acc done = run;
+#pragma unroll
+        for (int k = 0; k < CW; ++k) {
+            const bool at = k == h;
+            done = at ? run : done;
+            run = at ? P::zero() : run;
+            run = P::fma(v[k], x[k], run);
+        }
+        if (cb != 0u) {
+            if (cur_row >= 0)
+                store_row(a.y, a.m, cur_row, P::out_acc(done), a.err);
+            else
+                head = done;
+            cur_row = rowof[lane * S + kk0 + h];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < CW; ++k) {
+            if ((cb >> (CW - 1 - k)) & 1u) {
+                if (cur_row >= 0)
+                    store_row(a.y, a.m, cur_row, P::out_acc(run), a.err);  // complete in lane
+                else
+                    head = run;  // slots before the lane's first row head
+                cur_row = rowof[lane * S + kk0 + k];
+                run = P::zero();
+            }
+            run = P::fma(v[k], x[k], run);
+        }
+    }
+}
+
 // The tile kernel.  One warp = one worker over tiles [t_begin, t_end).  The stream runs as a
 // software pipeline over the worker's chunks of CW non-zeros per lane: while chunk g is
 // multiplied, the values of chunk g+1 and the column indices of chunk g+2 are in flight and the
 // x gathers of chunk g+1 are issued; the bit flags' row_ptr entries and tile_ptr are fetched
 // one tile ahead.
-template <class P, int S>
+template <class P, int S, bool OH = false>
 __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, int tpw, int ntiles,
                                             uint32_t* const s_words_w, int* const rowof) {
     using Acc = typename P::Acc;
@@ -230,6 +283,8 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     constexpr int TILE = 32 * S;
     constexpr int CW = chunk_width<S, typename P::XT>();
     constexpr int NC = S / CW;
+    // the one-head chunk form (scalar accumulators only; wide ones keep the per-slot loop)
+    constexpr bool one_head = OH && sizeof(Acc) <= 8;
     const int lane = threadIdx.x & 31;
     const int t_begin = worker * tpw;
     const int t_end = min(t_begin + tpw, ntiles);
@@ -329,20 +384,10 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
                 load_vals<P, S, CW>(a, t1, c1, lane, pol_s, valB);
                 gather_cw(a.x, colA, pol_x, xB);
             }
-            // multiply chunk g
-#pragma unroll
-            for (int k = 0; k < CW; ++k) {
-                const int kk = c * CW + k;
-                if ((w >> (31 - kk)) & 1u) {
-                    if (cur_row >= 0)
-                        store_row(a.y, a.m, cur_row, P::out_acc(run), a.err);  // complete in lane
-                    else
-                        head = run;  // slots before the lane's first row head
-                    cur_row = rowof[lane * S + kk];
-                    run = P::zero();
-                }
-                run = P::fma(valA[k], xA[k], run);
-            }
+            // multiply chunk g (its row-head bits: slot c*CW in bit CW-1)
+            const uint32_t cb = (w >> (32 - (c + 1) * CW)) & ((1u << CW) - 1u);
+            chunk_segments<P, S, CW>(one_head, cb, c * CW, valA, xA, run, head, cur_row, rowof,
+                                     lane, a);
 #pragma unroll
             for (int k = 0; k < CW; ++k) {
                 colA[k] = colB[k];
@@ -395,7 +440,7 @@ struct MinBlocks {
 };
 
 // One warp = one worker, worker = global warp index (static schedule).
-template <class P, int S, int WARPS>
+template <class P, int S, int WARPS, bool OH>
 __global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
     k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
     __shared__ uint32_t s_words[WARPS][32];
@@ -405,7 +450,7 @@ __global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
     const int warp = threadIdx.x >> 5;
     const int worker = blockIdx.x * WARPS + warp;
     if (worker >= nworkers) return;
-    tile_worker<P, S>(a, worker, tpw, ntiles, s_words[warp], s_rowof[warp]);
+    tile_worker<P, S, OH>(a, worker, tpw, ntiles, s_words[warp], s_rowof[warp]);
 }
 
 // Persistent schedule: a grid sized to the GPU's resident capacity; each warp takes the next
@@ -534,7 +579,14 @@ cudaError_t launch_tiles_t(const TileArgs<P>& a, int tpw, int nworkers, int ntil
                            cudaStream_t st) {
     if (nworkers > 0 && (a.phase & 1)) {
         const int blocks = (nworkers + WARPS - 1) / WARPS;
-        k_tiles<P, S, WARPS><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+        if constexpr (sizeof(typename P::Acc) <= 8) {  // scalar accumulators: either form
+            if (a.one_head)
+                k_tiles<P, S, WARPS, true><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+            else
+                k_tiles<P, S, WARPS, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+        } else {
+            k_tiles<P, S, WARPS, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+        }
     }
     if (a.phase & 2) {
         const cudaError_t e = launch_calibrate(a, nworkers, st);

@@ -120,7 +120,7 @@ __device__ __forceinline__ void gather8(const XT* __restrict__ x, const int (&c)
     for (int i = 0; i < 8; ++i) xv[i] = c[i] >= 0 ? ld_x(x + c[i], pol) : XT(0);
 }
 
-template <class P, int S, int WARPS, int NSTAGE>
+template <class P, int S, int WARPS, int NSTAGE, bool OH>
 __global__ void __launch_bounds__(WARPS * 32, 1)
     k_tiles_tma(TileArgs<P> a, const __grid_constant__ StreamMaps maps, int tpw, int nworkers,
                 int ntiles) {
@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     const int t_end = min(t_begin + tpw, ntiles);
     const uint64_t pol_s = policy_evict_first();
     const uint64_t pol_x = policy_evict_last();
+    constexpr bool one_head = OH && sizeof(Acc) <= 8;  // the one-head chunk form
     auto is_full = [&](int t) { return (long long)(t + 1) * TILE <= a.nnz; };
     auto vslot = [&](int t) { return wb + ((t - t_begin) % NSTAGE) * L::SLOT; };
 
@@ -289,19 +290,9 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
 #pragma unroll
                 for (int k = 0; k < 8; ++k) run = P::fma(v[k], xa[k], run);
             } else {
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const int kk = c * 8 + k;
-                    if ((w >> (31 - kk)) & 1u) {
-                        if (cur_row >= 0)
-                            store_row(a.y, a.m, cur_row, P::out_acc(run), a.err);
-                        else
-                            head = run;
-                        cur_row = rowof[lane * S + kk];
-                        run = P::zero();
-                    }
-                    run = P::fma(v[k], xa[k], run);
-                }
+                const uint32_t cb = (w >> (32 - (c + 1) * 8)) & 0xFFu;
+                chunk_segments<P, S, 8>(one_head, cb, c * 8, v, xa, run, head, cur_row, rowof,
+                                        lane, a);
             }
 #pragma unroll
             for (int k = 0; k < 8; ++k) xa[k] = xb[k];
@@ -357,6 +348,28 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     if (!rec_written && lane == 0) a.rec_row[worker] = -1;
 }
 
+template <class P, int S, int WARPS, int NSTAGE, bool OH>
+cudaError_t launch_tma_kernel(const TileArgs<P>& a, const StreamMaps& maps, int tpw, int nworkers,
+                              int ntiles, int bytes, cudaStream_t st) {
+    // the shared-memory opt-in is a per-device function attribute: set it once per device
+    // (setting it twice from racing host threads is harmless; the flag word is atomic)
+    static std::atomic<unsigned long long> attr_set{0ull};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(attr_set.load(std::memory_order_acquire) & bit)) {
+        e = cudaFuncSetAttribute(k_tiles_tma<P, S, WARPS, NSTAGE, OH>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        attr_set.fetch_or(bit, std::memory_order_release);
+    }
+    const int blocks = (nworkers + WARPS - 1) / WARPS;
+    k_tiles_tma<P, S, WARPS, NSTAGE, OH><<<blocks, WARPS * 32, bytes, st>>>(a, maps, tpw, nworkers,
+                                                                           ntiles);
+    return cudaSuccess;
+}
+
 template <class P, int S, int WARPS, int NSTAGE>
 cudaError_t launch_tiles_tma_t(const TileArgs<P>& a, int tpw, int nworkers, int ntiles,
                                cudaStream_t st) {
@@ -374,22 +387,16 @@ cudaError_t launch_tiles_tma_t(const TileArgs<P>& a, int tpw, int nworkers, int 
             TileConfig c{S, tpw, WARPS, 0};
             return launch_tiles<P>(a, c, st);
         }
-        // the shared-memory opt-in is a per-device function attribute: set it once per device
-        // (setting it twice from racing host threads is harmless; the flag word is atomic)
-        static std::atomic<unsigned long long> attr_set{0ull};
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
+        cudaError_t e;
+        if constexpr (sizeof(typename P::Acc) <= 8)  // scalar accumulators: either form
+            e = a.one_head ? launch_tma_kernel<P, S, WARPS, NSTAGE, true>(a, maps, tpw, nworkers,
+                                                                         ntiles, bytes, st)
+                           : launch_tma_kernel<P, S, WARPS, NSTAGE, false>(a, maps, tpw, nworkers,
+                                                                          ntiles, bytes, st);
+        else
+            e = launch_tma_kernel<P, S, WARPS, NSTAGE, false>(a, maps, tpw, nworkers, ntiles,
+                                                              bytes, st);
         if (e != cudaSuccess) return e;
-        const unsigned long long bit = 1ull << (dev & 63);
-        if (!(attr_set.load(std::memory_order_acquire) & bit)) {
-            e = cudaFuncSetAttribute(k_tiles_tma<P, S, WARPS, NSTAGE>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-            if (e != cudaSuccess) return e;
-            attr_set.fetch_or(bit, std::memory_order_release);
-        }
-        const int blocks = (nworkers + WARPS - 1) / WARPS;
-        k_tiles_tma<P, S, WARPS, NSTAGE>
-            <<<blocks, WARPS * 32, bytes, st>>>(a, maps, tpw, nworkers, ntiles);
     }
     if (a.phase & 2) {
         const cudaError_t e = launch_calibrate(a, nworkers, st);

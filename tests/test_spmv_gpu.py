@@ -227,6 +227,68 @@ def test_plan_api_on_torch_tensors(cuda_ok):
     del rng
 
 
+def _long_rows_with_short(rng, m, n, long_len=27, short_every=100, empty_every=211):
+    """Integer CSR: rows of long_len non-zeros, every short_every-th row 1..7 long (two row
+    heads in one lane's chunk), every empty_every-th row empty (dirty tiles)."""
+    lens = np.full(m, long_len)
+    lens[::short_every] = rng.integers(1, 8, lens[::short_every].size)
+    lens[5::empty_every] = 0
+    rp = np.zeros(m + 1, np.int32)
+    rp[1:] = np.cumsum(lens)
+    col = np.concatenate([np.sort(rng.choice(n, int(l), replace=False)) for l in lens]
+                         ).astype(np.int32)
+    val = rng.integers(-9, 10, int(rp[-1])).astype(np.float64)
+    x = rng.integers(-9, 10, n).astype(np.float64)
+    return rp, col, val, x
+
+
+def _chunk_form(rp, col, vt, seg):
+    import torch
+    p = sp.Plan(vt, rp.size - 1, int(col.max()) + 1 if col.size else 1,
+                torch.from_numpy(rp).cuda(), torch.from_numpy(col).cuda(), seg=seg)
+    try:
+        return p.chunk_form()
+    finally:
+        p.close()
+
+
+@pytest.mark.parametrize("seg", [8, 16, 32])
+def test_one_head_chunk_form_decision(cuda_ok, seg):
+    """The plan counts the non-empty rows shorter than a chunk (4 slots at seg 8, else 8) and
+    takes the one-head form when they can break at most 1/8 of the warp-chunks."""
+    rng = np.random.default_rng(5)
+    cw = 4 if seg == 8 else 8
+    for a, expect in ((gen.stencil3d(24, 20, 17, seed=3), True), (gen.powerlaw(30000, seed=4), False)):
+        lens = np.diff(a.row_ptr)
+        short = int(np.count_nonzero((lens > 0) & (lens < cw)))
+        got_short, on = _chunk_form(a.row_ptr, a.col, sp.VALUE_F64, seg)
+        assert got_short == short
+        chunks = -(-int(a.row_ptr[-1]) // (32 * cw))
+        assert on == (8 * short <= chunks) == expect
+    rp, col, _, _ = _long_rows_with_short(rng, 20000, 30000)
+    lens = np.diff(rp)
+    got_short, on = _chunk_form(rp, col, sp.VALUE_F64, seg)
+    assert got_short == int(np.count_nonzero((lens > 0) & (lens < cw))) and on
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_one_head_form_with_fallback_chunks_bit_exact(cuda_ok, cfg):
+    """Long rows with sparse short and empty rows: most chunks take the one-head form, the
+    chunks where a short row puts two heads into one lane take the per-slot loop, in the
+    same launch.  Integer data: bit-exact against the serial loop."""
+    rng = np.random.default_rng(cfg[0] * 100 + cfg[1] * 10 + cfg[3])
+    rp, col, val, x = _long_rows_with_short(rng, 20000, 30000)
+    assert _chunk_form(rp, col, sp.VALUE_F64, cfg[0])[1]
+    yr = oracle.csr_serial(rp, col, val, x)
+    for vt in (sp.VALUE_F64, sp.VALUE_F32):
+        y = run_handle(vt, rp, col, val, x, cfg)
+        assert np.array_equal(y, yr.astype(sp.host_dtype(vt)))
+    ystar = oracle.csr_dot2(rp, col, val, x)
+    for vt in (sp.VALUE_MIXED_F32, sp.VALUE_MIXED_BF16):
+        y = run_handle(vt, rp, col, val, x, cfg)
+        assert oracle.normwise_error(y, ystar) <= TOL_MIXED_NORMWISE
+
+
 def test_set_x_reuses_the_matrix(cuda_ok):
     a = gen.stencil2d(64, 64)
     x1, x2 = gen.uniform(a.n, 1), gen.uniform(a.n, 2)
