@@ -444,7 +444,9 @@ def run_ours(args) -> None:
 
 def measure_forms(args, a, x, ystar) -> dict:
     """The other value types on the same workload: device GB/s on their own algorithmic
-    bytes, non-zeros/s, and their error against the FP64 oracle."""
+    bytes, non-zeros/s, and their error against the FP64 oracle.  Each form runs the faster
+    of its default schedule and the autotuner's pick for it (the autotuner's candidates load
+    the stream directly; BF16 storage defaults to the TMA-staged ring)."""
     import numpy as np
     import torch
 
@@ -454,35 +456,63 @@ def measure_forms(args, a, x, ystar) -> dict:
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
     steps = max(10, min(args.steps, 50))
     for vt, sv, sx in ((sp.VALUE_F32, 4, 4), (sp.VALUE_MIXED_F32, 4, 4), (sp.VALUE_MIXED_BF16, 2, 4)):
-        h = sp.BhsparseSpmvCuda(vt)
-        dt = sp.host_dtype(vt)
-        y = np.zeros(a.m, dt)
-        if h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val.astype(dt), x.astype(dt), y):
-            out[sp.VALUE_NAMES[vt]] = {"error": h.last_error}
+        pick = tuple(autotune_workload(a, x, vt)["pick"])
+        dh = sp.BhsparseSpmvCuda(vt)
+        default = dh.get_config()
+        dh.close()
+        best = None
+        for cfg in dict.fromkeys((pick, default)):
+            r = _time_form(vt, cfg, a, x, flush, steps)
+            if "error" in r or best is None or r["ms"] < best[1]["ms"]:
+                best = (cfg, r)
+            if "error" in r:
+                break
+        cfg, r = best
+        if "error" in r:
+            out[sp.VALUE_NAMES[vt]] = {"error": r["error"]}
             continue
-        stream = torch.cuda.Stream()
-        with torch.cuda.stream(stream):
-            for _ in range(5):
-                h.run_phase(stream.cuda_stream, 3)
-            evs = []
-            for i in range(steps):
-                flush.fill_(i & 0xFF)
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                h.run_phase(stream.cuda_stream, 3)
-                e1.record(stream)
-                evs.append((e0, e1))
-        torch.cuda.synchronize()
-        assert h.check() == 0, h.last_error
-        ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in evs)
-        assert h.get_y() == 0
+        ms, y = r["ms"], r["y"]
         Bf = alg_bytes(a.m, a.n, a.nnz, sv, sx, 4)
         out[sp.VALUE_NAMES[vt]] = {
             "gbs": round(Bf / (ms * 1e-3) / 1e9, 1), "ms_per_step": round(ms, 5),
-            "gnnz_per_s": round(a.nnz / (ms * 1e-3) / 1e9, 2),
+            "gnnz_per_s": round(a.nnz / (ms * 1e-3) / 1e9, 2), "schedule": list(cfg),
             "normwise_err_vs_fp64_oracle": oracle.normwise_error(y, ystar)}
-        h.close()
     return out
+
+
+def _time_form(vt, cfg, a, x, flush, steps) -> dict:
+    """Whole steps of one value type at one schedule through the handle (L2 flushed before
+    each, CUDA events): {"ms", "y"} or {"error"}."""
+    import numpy as np
+    import torch
+
+    import benchmark_spmv_using_csr_gb300 as sp
+    h = sp.BhsparseSpmvCuda(vt)
+    assert h.set_config(*cfg) == 0, h.last_error
+    dt = sp.host_dtype(vt)
+    y = np.zeros(a.m, dt)
+    if h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val.astype(dt), x.astype(dt), y):
+        err = h.last_error
+        h.close()
+        return {"error": err}
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        for _ in range(5):
+            h.run_phase(stream.cuda_stream, 3)
+        evs = []
+        for i in range(steps):
+            flush.fill_(i & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            h.run_phase(stream.cuda_stream, 3)
+            e1.record(stream)
+            evs.append((e0, e1))
+    torch.cuda.synchronize()
+    assert h.check() == 0, h.last_error
+    ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in evs)
+    assert h.get_y() == 0
+    h.close()
+    return {"ms": ms, "y": y}
 
 
 def measure_fp64(args, a, x, config=None) -> dict:
@@ -619,17 +649,22 @@ def cpu_openmp(a, x, B, seconds: float) -> dict:
     return out
 
 
-def autotune_workload(a, x) -> dict:
+def autotune_workload(a, x, vt=None) -> dict:
     """Run the library's autotuner (every candidate schedule, median of 11 timed runs, L2
-    flushed before each) on the workload and return its table and pick."""
+    flushed before each) on the workload in value type vt (plain FP64 by default) and return
+    its table and pick."""
     import torch
 
     import benchmark_spmv_using_csr_gb300 as sp
     from benchmark_spmv_using_csr_gb300 import tune
+    vt = sp.VALUE_F64 if vt is None else vt
     rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
     val, xd = torch.from_numpy(a.val).cuda(), torch.from_numpy(x).cuda()
-    y = torch.zeros(a.m, dtype=torch.float64, device="cuda")
-    ms, best = tune.autotune(sp.VALUE_F64, rp, ci, val, xd, y, warmup=2, reps=11)
+    if vt != sp.VALUE_F64:  # storage types of the other forms; x and y in FP32
+        val = val.to(torch.bfloat16 if vt == sp.VALUE_MIXED_BF16 else torch.float32)
+        xd = xd.float()
+    y = torch.zeros(a.m, dtype=xd.dtype, device="cuda")
+    ms, best = tune.autotune(vt, rp, ci, val, xd, y, warmup=2, reps=11)
     cands = tune.candidates()
     del rp, ci, val, xd, y
     torch.cuda.empty_cache()
