@@ -95,6 +95,13 @@ __device__ __forceinline__ void gather_cw(const XT* __restrict__ x, const int (&
 #pragma unroll
     for (int i = 0; i < CW; ++i) xv[i] = c[i] >= 0 ? ld_x(x + c[i], pol) : XT(0);
 }
+// x entries of a chunk of a full tile, which has no padding slot (column -1) to test
+template <int CW, typename XT>
+__device__ __forceinline__ void gather_cw_full(const XT* __restrict__ x, const int (&c)[CW],
+                                               uint64_t pol, XT (&xv)[CW]) {
+#pragma unroll
+    for (int i = 0; i < CW; ++i) xv[i] = ld_x(x + c[i], pol);
+}
 
 template <typename YT>
 __device__ __forceinline__ void store_row(YT* y, int m, int row, YT v, uint32_t* err) {
@@ -382,7 +389,12 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
             if (t2 < t_end) load_cols<P, S, CW>(a, t2, c2, lane, pol_s, colB);
             if (t1 < t_end) {
                 load_vals<P, S, CW>(a, t1, c1, lane, pol_s, valB);
-                gather_cw(a.x, colA, pol_x, xB);
+                // the one-head kernels gather a full tile's x without the padding test (1 %
+                // on the 27-point stencil; the per-slot kernels measured no gain from it)
+                if (one_head && (long long)(t1 + 1) * TILE <= a.nnz)
+                    gather_cw_full(a.x, colA, pol_x, xB);
+                else
+                    gather_cw(a.x, colA, pol_x, xB);
             }
             // multiply chunk g (its row-head bits: slot c*CW in bit CW-1)
             const uint32_t cb = (w >> (32 - (c + 1) * CW)) & ((1u << CW) - 1u);
