@@ -289,6 +289,37 @@ def test_one_head_form_with_fallback_chunks_bit_exact(cuda_ok, cfg):
         assert oracle.normwise_error(y, ystar) <= TOL_MIXED_NORMWISE
 
 
+@pytest.mark.parametrize("cfg", [(8, 3, 4, 0), (16, 4, 4, 0), (32, 4, 4, 0), (32, 2, 8, 0),
+                                 (16, 2, 4, 2), (32, 1, 4, 3)])
+@pytest.mark.parametrize("long_rows", [True, False])
+def test_inf_and_nan_propagate_like_the_serial_loop(cuda_ok, cfg, long_rows):
+    """Inf and NaN in x and in the values reach exactly the rows of the serial loop
+    (spmv_cuda/main.cu:755-761): a row is NaN where the loop's is NaN, +-Inf where it is, and
+    every finite row is bit-exact (integer data).  Long rows take the one-head chunk form,
+    short ones the per-slot loop."""
+    rng = np.random.default_rng(cfg[0] * 10 + cfg[3] + (100 if long_rows else 0))
+    if long_rows:
+        rp, col, val, x = _long_rows_with_short(rng, 12000, 20000)
+    else:
+        rp, col, val, x = int_csr(rng, m=12000, n=20000, maxlen=12, empty=0.05)
+    x[rng.choice(x.size, 6, replace=False)] = [np.inf, -np.inf, np.nan, np.inf, -np.inf, np.nan]
+    val[rng.choice(val.size, 4, replace=False)] = [np.inf, -np.inf, np.nan, np.inf]
+    yr = oracle.csr_serial(rp, col, val, x)
+    assert np.isnan(yr).any() and np.isinf(yr).any()
+    for vt in (sp.VALUE_F64, sp.VALUE_F32):
+        y = run_handle(vt, rp, col, val, x, cfg).astype(np.float64)
+        assert np.array_equal(np.isnan(y), np.isnan(yr))
+        assert np.array_equal(np.isposinf(y), np.isposinf(yr))
+        assert np.array_equal(np.isneginf(y), np.isneginf(yr))
+        fin = np.isfinite(yr)
+        assert np.array_equal(y[fin], yr[fin].astype(sp.host_dtype(vt)))
+    # compensated accumulation turns an infinite row into NaN (TwoSum's error term of an
+    # infinite sum is inf - inf); the finite rows stay finite and the others do not
+    for vt in (sp.VALUE_MIXED_F32, sp.VALUE_MIXED_BF16):
+        y = run_handle(vt, rp, col, val, x, cfg).astype(np.float64)
+        assert np.array_equal(np.isfinite(y), np.isfinite(yr))
+
+
 def test_set_x_reuses_the_matrix(cuda_ok):
     a = gen.stencil2d(64, 64)
     x1, x2 = gen.uniform(a.n, 1), gen.uniform(a.n, 2)
