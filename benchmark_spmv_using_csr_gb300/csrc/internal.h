@@ -23,11 +23,13 @@ cudaError_t launch_bitflags(const int* row_ptr, int m, int nnz, int seg, const u
                             uint32_t* words, cudaStream_t st);
 // *count = non-empty rows shorter than cw non-zeros (zeroed first)
 cudaError_t launch_short_rows(const int* row_ptr, int m, int cw, uint32_t* count, cudaStream_t st);
-// Whether the tile kernels take the one-head chunk form: the short rows can break at most 1/8
-// of the warp-chunks (32 lanes x cw slots).
+// Whether the tile kernels take the one-head chunk form: the short rows can break at most 1/4
+// of the warp-chunks (32 lanes x cw slots).  Measured on rows of 27 non-zeros with a share of
+// 1-3-entry rows: the form still wins where they could break half of the chunks (1.00-1.06x),
+// loses where they can break all of them, and is mixed in between.
 inline bool one_head_pays(long long short_rows, long long nnz, int cw) {
     const long long chunks = (nnz + 32LL * cw - 1) / (32LL * cw);
-    return 8 * short_rows <= chunks;
+    return 4 * short_rows <= chunks;
 }
 cudaError_t launch_validate(const int* row_ptr, const int* col, int m, int n, int nnz,
                             uint32_t* bad, cudaStream_t st);

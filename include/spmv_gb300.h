@@ -141,7 +141,7 @@ int bhsp_plan_launches(const bhsp_plan* p);
 int bhsp_plan_tiles(const bhsp_plan* p, const uint32_t** d_tile_ptr, int* ntiles, int* tile_nnz);
 /* The chunk form the plan's tile kernel takes, fixed when the plan is built: *short_rows =
  * non-empty rows shorter than one chunk of a lane's slots (4 at seg 8, else 8), *one_head = 1
- * when they are few enough (at most 1/8 of the warp-chunks) for the branch-free one-head form. */
+ * when they are few enough (at most 1/4 of the warp-chunks) for the branch-free one-head form. */
 int bhsp_plan_chunk_form(const bhsp_plan* p, int* short_rows, int* one_head);
 const char* bhsp_plan_last_error(const bhsp_plan* p);
 void bhsp_plan_destroy(bhsp_plan* p);

@@ -255,7 +255,7 @@ def _chunk_form(rp, col, vt, seg):
 @pytest.mark.parametrize("seg", [8, 16, 32])
 def test_one_head_chunk_form_decision(cuda_ok, seg):
     """The plan counts the non-empty rows shorter than a chunk (4 slots at seg 8, else 8) and
-    takes the one-head form when they can break at most 1/8 of the warp-chunks."""
+    takes the one-head form when they can break at most 1/4 of the warp-chunks."""
     rng = np.random.default_rng(5)
     cw = 4 if seg == 8 else 8
     for a, expect in ((gen.stencil3d(24, 20, 17, seed=3), True), (gen.powerlaw(30000, seed=4), False)):
@@ -264,7 +264,7 @@ def test_one_head_chunk_form_decision(cuda_ok, seg):
         got_short, on = _chunk_form(a.row_ptr, a.col, sp.VALUE_F64, seg)
         assert got_short == short
         chunks = -(-int(a.row_ptr[-1]) // (32 * cw))
-        assert on == (8 * short <= chunks) == expect
+        assert on == (4 * short <= chunks) == expect
     rp, col, _, _ = _long_rows_with_short(rng, 20000, 30000)
     lens = np.diff(rp)
     got_short, on = _chunk_form(rp, col, sp.VALUE_F64, seg)
