@@ -5,6 +5,7 @@
 // x is gathered through the read-only path (ld.global.nc) with an L2 evict-last policy.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
