@@ -279,7 +279,7 @@ __device__ __forceinline__ void chunk_segments(bool one_head, uint32_t cb, int k
 // multiplied, the values of chunk g+1 and the column indices of chunk g+2 are in flight and the
 // x gathers of chunk g+1 are issued; the bit flags' row_ptr entries and tile_ptr are fetched
 // one tile ahead.
-template <class P, int S, bool OH = false>
+template <class P, int S, bool OH = false, bool MID = false>
 __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, int tpw, int ntiles,
                                             uint32_t* const s_words_w, int* const rowof) {
     using Acc = typename P::Acc;
@@ -340,10 +340,15 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     // +3 % on both benchmark matrices.  The FP32 and mixed forms build each tile's words at its
     // start (building them early cost them 2-6 %).
     constexpr bool early_flags = std::is_same<VC, double>::value && sizeof(Acc) == 8;
+    // MID (the caller gave two map buffers): the next tile's words are built half-way through
+    // this tile's chunk loop, into the other buffer, overlapping the FMA chain as well
+    constexpr bool mid_flags = MID && early_flags;
+    int* rowof_cur = rowof;
+    int* rowof_nxt = rowof + (mid_flags ? TILE : 0);
     uint32_t w_next = 0u;
     if constexpr (early_flags)
         w_next = tile_rows<S, YT>(a.row_ptr, a.m, t_begin * TILE, (int)(tp0 & ROW_MASK),
-                                  (int)(tp1 & ROW_MASK), rb, s_words_w, rowof, a.y);
+                                  (int)(tp1 & ROW_MASK), rb, s_words_w, rowof_cur, a.y);
     for (int t = t_begin; t < t_end; ++t) {
         const int lo = (int)(tp0 & ROW_MASK);
         const int hi = (int)(tp1 & ROW_MASK);
@@ -357,7 +362,7 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
         if constexpr (early_flags)
             w = w_next;
         else
-            w = tile_rows<S, YT>(a.row_ptr, a.m, t * TILE, lo, hi, rb, s_words_w, rowof, a.y);
+            w = tile_rows<S, YT>(a.row_ptr, a.m, t * TILE, lo, hi, rb, s_words_w, rowof_cur, a.y);
         const bool first_head = ((__shfl_sync(SPMV_FULL_MASK, w, 0) >> 31) & 1u) != 0u;
         const uint32_t fmask = __ballot_sync(SPMV_FULL_MASK, w != 0u);
 
@@ -411,8 +416,14 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
             }
             // multiply chunk g (its row-head bits: slot c*CW in bit CW-1)
             const uint32_t cb = (w >> (32 - (c + 1) * CW)) & ((1u << CW) - 1u);
-            chunk_segments<P, S, CW>(one_head, cb, c * CW, valA, xA, run, head, cur_row, rowof,
-                                     lane, a);
+            chunk_segments<P, S, CW>(one_head, cb, c * CW, valA, xA, run, head, cur_row,
+                                     rowof_cur, lane, a);
+            if constexpr (mid_flags) {
+                if (c == NC / 2 - 1 && t + 1 < t_end)
+                    w_next = tile_rows<S, YT>(a.row_ptr, a.m, (t + 1) * TILE, hi,
+                                              (int)(tp2 & ROW_MASK), rbn, s_words_w, rowof_nxt,
+                                              a.y);
+            }
 #pragma unroll
             for (int k = 0; k < CW; ++k) {
                 colA[k] = colB[k];
@@ -421,10 +432,14 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
             }
         }
         __syncwarp();  // rowof / s_words are rebuilt next
-        if constexpr (early_flags) {
+        if constexpr (mid_flags) {
+            int* const t_ = rowof_cur;
+            rowof_cur = rowof_nxt;
+            rowof_nxt = t_;
+        } else if constexpr (early_flags) {
             if (t + 1 < t_end)
                 w_next = tile_rows<S, YT>(a.row_ptr, a.m, (t + 1) * TILE, hi,
-                                          (int)(tp2 & ROW_MASK), rbn, s_words_w, rowof, a.y);
+                                          (int)(tp2 & ROW_MASK), rbn, s_words_w, rowof_cur, a.y);
         } else {
             rb = rbn;
         }
@@ -475,14 +490,20 @@ struct MinBlocks {
 template <class P, int S, int WARPS, bool OH>
 __global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
     k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
+    // Plain FP64 with the one-head form (long rows) keeps two slot -> row maps per warp where
+    // they fit in 40 KB (all but S = 32 at 8 warps), so that the next tile's map is built half-
+    // way through this tile's chunk loop: +1.4 % on the 27-point stencil at (32, 4, 4).  The
+    // per-slot form builds it after the loop: half-way cost the power-law matrix 5-9 %.
+    constexpr bool MID = OH && std::is_same<typename P::VC, double>::value &&
+                         sizeof(typename P::Acc) == 8 && WARPS * 2 * 32 * S * 4 <= 40 * 1024;
     __shared__ uint32_t s_words[WARPS][32];
-    __shared__ int s_rowof[WARPS][32 * S];
+    __shared__ int s_rowof[WARPS][(MID ? 2 : 1) * 32 * S];
     // the calibration kernel may be scheduled now; it waits for this grid's completion itself
     asm volatile("griddepcontrol.launch_dependents;");
     const int warp = threadIdx.x >> 5;
     const int worker = blockIdx.x * WARPS + warp;
     if (worker >= nworkers) return;
-    tile_worker<P, S, OH>(a, worker, tpw, ntiles, s_words[warp], s_rowof[warp]);
+    tile_worker<P, S, OH, MID>(a, worker, tpw, ntiles, s_words[warp], s_rowof[warp]);
 }
 
 // Persistent schedule: a grid sized to the GPU's resident capacity; each warp takes the next
