@@ -145,6 +145,29 @@ __device__ __forceinline__ void load_cols(const TileArgs<P>& a, int t, int c, in
         for (int i = 0; i < CW; ++i) cc[i] = e + i < a.nnz ? a.col[e + i] : -1;
     }
 }
+// S = 8: a lane's 8 column indices of tile t (one 32-byte sector) in one load, split into the
+// tile's two 4-slot chunks.  Two 16-byte loads a chunk apart read the sector twice when the x
+// gathers in between evict it from L1.
+template <class P>
+__device__ __forceinline__ void load_cols_tile8(const TileArgs<P>& a, int t, int lane, uint64_t pol,
+                                                int (&c0)[4], int (&c1)[4]) {
+    const int e = t * 256 + lane * 8;
+    if ((long long)(t + 1) * 256 <= a.nnz) {
+        uint32_t u[8];
+        ld_stream_b32x8(a.col + e, pol, u);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            c0[i] = (int)u[i];
+            c1[i] = (int)u[4 + i];
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            c0[i] = e + i < a.nnz ? a.col[e + i] : -1;
+            c1[i] = e + 4 + i < a.nnz ? a.col[e + 4 + i] : -1;
+        }
+    }
+}
 template <int CW>
 __device__ __forceinline__ void load_vals_full(const double* val, int e, uint64_t pol,
                                                double (&v)[CW]) {
@@ -343,6 +366,11 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     // MID (the caller gave two map buffers): the next tile's words are built half-way through
     // this tile's chunk loop, into the other buffer, overlapping the FMA chain as well
     constexpr bool mid_flags = MID && early_flags;
+    // S = 8 (4-slot chunks): a tile's column indices per lane are one sector, loaded whole (+2 %
+    // on the power-law matrix in every form; the FP64 kernels that build flags half-way lost
+    // 7 % with it and keep two 16-byte loads)
+    constexpr bool whole_col_sector = S == 8 && CW == 4 && !mid_flags;
+    int colC[CW];  // the next tile's second column chunk, loaded with its first
     int* rowof_cur = rowof;
     int* rowof_nxt = rowof + (mid_flags ? TILE : 0);
     uint32_t w_next = 0u;
@@ -404,7 +432,16 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
             // issue: columns of chunk g+2, values and x of chunk g+1
             const int t1 = t + (c + 1) / NC, c1 = (c + 1) % NC;
             const int t2 = t + (c + 2) / NC, c2 = (c + 2) % NC;
-            if (t2 < t_end) load_cols<P, S, CW>(a, t2, c2, lane, pol_s, colB);
+            if constexpr (whole_col_sector) {
+                if (c == 0) {  // the next tile's columns, both chunks
+                    if (t + 1 < t_end) load_cols_tile8(a, t + 1, lane, pol_s, colB, colC);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < CW; ++k) colB[k] = colC[k];
+                }
+            } else {
+                if (t2 < t_end) load_cols<P, S, CW>(a, t2, c2, lane, pol_s, colB);
+            }
             if (t1 < t_end) {
                 load_vals<P, S, CW>(a, t1, c1, lane, pol_s, valB);
                 // the one-head kernels gather a full tile's x without the padding test (1 %
