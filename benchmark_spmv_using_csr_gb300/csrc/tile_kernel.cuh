@@ -187,6 +187,28 @@ __device__ __forceinline__ void load_vals_full(const float* val, int e, uint64_t
 #pragma unroll
     for (int i = 0; i < CW; ++i) v[i] = __uint_as_float(u[i]);
 }
+// S = 8, 4-byte values: a lane's 8 values of tile t (one 32-byte sector) in one load, split into
+// the tile's two 4-slot chunks
+template <class P>
+__device__ __forceinline__ void load_vals_tile8(const TileArgs<P>& a, int t, int lane, uint64_t pol,
+                                                typename P::VC (&v0)[4], typename P::VC (&v1)[4]) {
+    const int e = t * 256 + lane * 8;
+    if ((long long)(t + 1) * 256 <= a.nnz) {
+        uint32_t u[8];
+        ld_stream_b32x8(a.val + e, pol, u);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            v0[i] = __uint_as_float(u[i]);
+            v1[i] = __uint_as_float(u[4 + i]);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            v0[i] = e + i < a.nnz ? to_compute(a.val[e + i]) : typename P::VC(0);
+            v1[i] = e + 4 + i < a.nnz ? to_compute(a.val[e + 4 + i]) : typename P::VC(0);
+        }
+    }
+}
 template <int CW>
 __device__ __forceinline__ void load_vals_full(const __nv_bfloat16* val, int e, uint64_t pol,
                                                float (&v)[CW]) {
@@ -329,10 +351,17 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     int colA[CW], colB[CW];
     VC valA[CW], valB[CW];
     XT xA[CW], xB[CW];
+    // S = 8 with 4-byte values (FP32 storage): a tile's values per lane are one sector, loaded
+    // whole like the column indices; valC holds the tile's second chunk until it is due
+    constexpr bool whole_val_sector = S == 8 && CW == 4 && sizeof(typename P::VS) == 4;
+    VC valC[CW];
     {
         int col0[CW];
         load_cols<P, S, CW>(a, t_begin, 0, lane, pol_s, col0);
-        load_vals<P, S, CW>(a, t_begin, 0, lane, pol_s, valA);
+        if constexpr (whole_val_sector)
+            load_vals_tile8(a, t_begin, lane, pol_s, valA, valC);
+        else
+            load_vals<P, S, CW>(a, t_begin, 0, lane, pol_s, valA);
         gather_cw(a.x, col0, pol_x, xA);
         const int t1 = t_begin + (NC > 1 ? 0 : 1);
         const int c1 = NC > 1 ? 1 : 0;
@@ -443,7 +472,16 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
                 if (t2 < t_end) load_cols<P, S, CW>(a, t2, c2, lane, pol_s, colB);
             }
             if (t1 < t_end) {
-                load_vals<P, S, CW>(a, t1, c1, lane, pol_s, valB);
+                if constexpr (whole_val_sector) {
+                    if (c == 0) {  // the tile's second chunk, loaded with its first
+#pragma unroll
+                        for (int k = 0; k < CW; ++k) valB[k] = valC[k];
+                    } else {  // the next tile's values, both chunks
+                        load_vals_tile8(a, t1, lane, pol_s, valB, valC);
+                    }
+                } else {
+                    load_vals<P, S, CW>(a, t1, c1, lane, pol_s, valB);
+                }
                 // the one-head kernels gather a full tile's x without the padding test (1 %
                 // on the 27-point stencil; the per-slot kernels measured no gain from it)
                 if (one_head && (long long)(t1 + 1) * TILE <= a.nnz)
