@@ -169,14 +169,23 @@ struct PolMixedK {
     }
 };
 
+// the persistent kernel for K right-hand sides: register-capped from 4 on
+template <int K, int S, int WARPS>
+constexpr auto persistent_kernel() {
+    if constexpr (K >= 4)
+        return &k_tiles_persistent_capped<PolMixedK<K>, S, WARPS>;
+    else
+        return &k_tiles_persistent<PolMixedK<K>, S, WARPS>;
+}
+
 template <int K, int S, int WARPS>
 static cudaError_t enqueue_batched(const TileArgs<PolMixedK<K>>& a, int tpw, int nworkers,
                                    int ntiles, int* ticket, int grid, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
     if (nworkers > 0)
-        k_tiles_persistent<PolMixedK<K>, S, WARPS><<<grid, WARPS * 32, 0, st>>>(a, tpw, nworkers,
-                                                                               ntiles, ticket);
+        persistent_kernel<K, S, WARPS>()<<<grid, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles,
+                                                                     ticket);
     int cb = (nworkers + 255) / 256;
     if (cb < 1) cb = 1;
     if (cb > 152 * 8) cb = 152 * 8;
@@ -191,7 +200,7 @@ static int persistent_grid() {
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_tiles_persistent<PolMixedK<K>, S, WARPS>, WARPS * 32, 0) != cudaSuccess)
+            &per_sm, persistent_kernel<K, S, WARPS>(), WARPS * 32, 0) != cudaSuccess)
         return 0;
     return sms * (per_sm > 0 ? per_sm : 1);
 }

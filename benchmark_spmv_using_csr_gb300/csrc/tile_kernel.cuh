@@ -584,12 +584,11 @@ __global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
 // Persistent schedule: a grid sized to the GPU's resident capacity; each warp takes the next
 // worker index from a global ticket until none is left (the global tile work queue of the
 // batched form: workers are consecutive tile ranges, so the ticket walks the tiles in order).
-template <class P, int S, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
-    k_tiles_persistent(TileArgs<P> a, int tpw, int nworkers, int ntiles, int* ticket) {
-    __shared__ uint32_t s_words[WARPS][32];
-    __shared__ int s_rowof[WARPS][32 * S];
-    const int warp = threadIdx.x >> 5;
+// The persistent loop: each warp takes the next worker index from the ticket until none is left.
+template <class P, int S>
+__device__ __forceinline__ void persistent_workers(const TileArgs<P>& a, int tpw, int nworkers,
+                                                   int ntiles, int* ticket, uint32_t* s_words_w,
+                                                   int* rowof) {
     const int lane = threadIdx.x & 31;
     for (;;) {
         int w = 0;
@@ -600,9 +599,32 @@ __global__ void __launch_bounds__(WARPS * 32)
             if (lane == 0) atomicOr(a.err, ERR_QUEUE);
             break;
         }
-        tile_worker<P, S>(a, w, tpw, ntiles, s_words[warp], s_rowof[warp]);
+        tile_worker<P, S>(a, w, tpw, ntiles, s_words_w, rowof);
         __syncwarp();
     }
+}
+
+template <class P, int S, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+    k_tiles_persistent(TileArgs<P> a, int tpw, int nworkers, int ntiles, int* ticket) {
+    __shared__ uint32_t s_words[WARPS][32];
+    __shared__ int s_rowof[WARPS][32 * S];
+    const int warp = threadIdx.x >> 5;
+    persistent_workers<P, S>(a, tpw, nworkers, ntiles, ticket, s_words[warp], s_rowof[warp]);
+}
+
+// The same with 16 resident warps per SM asked of the register allocator (128 registers), for
+// the accumulators of 4 and 8 right-hand sides: +1 % and +5 % on the batched workload (8
+// right-hand sides take 148 registers and 12 warps uncapped, a 48-byte spill capped).  One and
+// two right-hand sides keep the uncapped kernel: any explicit minimum changed their code and
+// cost one right-hand side 3-14 %.
+template <class P, int S, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
+    k_tiles_persistent_capped(TileArgs<P> a, int tpw, int nworkers, int ntiles, int* ticket) {
+    __shared__ uint32_t s_words[WARPS][32];
+    __shared__ int s_rowof[WARPS][32 * S];
+    const int warp = threadIdx.x >> 5;
+    persistent_workers<P, S>(a, tpw, nworkers, ntiles, ticket, s_words[warp], s_rowof[warp]);
 }
 
 // Exchange of any carry-record type between lanes (as 32-bit words).
