@@ -354,7 +354,7 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     // S = 8 with 4-byte values (FP32 storage): a tile's values per lane are one sector, loaded
     // whole like the column indices; valC holds the tile's second chunk until it is due
     constexpr bool whole_val_sector = S == 8 && CW == 4 && sizeof(typename P::VS) == 4;
-    VC valC[CW];
+    VC valC[CW] = {};
     {
         int col0[CW];
         load_cols<P, S, CW>(a, t_begin, 0, lane, pol_s, col0);
@@ -399,7 +399,9 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     // on the power-law matrix in every form; the FP64 kernels that build flags half-way lost
     // 7 % with it and keep two 16-byte loads)
     constexpr bool whole_col_sector = S == 8 && CW == 4 && !mid_flags;
-    int colC[CW];  // the next tile's second column chunk, loaded with its first
+    // the next tile's second column chunk, loaded with its first (copied on a worker's last tile
+    // without a load, but then never used; initialising it costs the S = 8 FP64 kernel a spill)
+    int colC[CW];
     int* rowof_cur = rowof;
     int* rowof_nxt = rowof + (mid_flags ? TILE : 0);
     uint32_t w_next = 0u;
