@@ -174,7 +174,8 @@ int bhsp_validate_csr(const int* d_row_ptr, const int* d_col_idx, int m, int n, 
  *                         (32-byte aligned).
  * x is [n_total][k] and y is [m_total][k], the k values of a row interleaved.  One persistent
  * kernel hands out tile ranges from a global ticket; schedule fields as in bhsp_set_config
- * (0 = default).  Validates the CSR and builds the partition (synchronous). */
+ * (0 = default: seg 16, or 32 for k = 4; 4 tiles per worker; 4 warps per CTA).  Validates the
+ * CSR and builds the partition (synchronous). */
 typedef struct bhsp_batch bhsp_batch;
 int bhsp_batch_create(bhsp_batch** out, int count, int m_total, int n_total, int nnz_total,
                       const int* d_row_ptr, const int* d_col_idx, int k, int seg,
