@@ -5,17 +5,20 @@
 //
 //  * the per-tile binary search moves to a one-off tile_ptr with dirty bits
 //    (partition.cu), read here with two loads per tile;
-//  * bit flags come from tile_flags() (tile.cuh), the same code the parity kernel runs;
-//  * each lane streams its own S consecutive non-zeros with 256-bit loads (evict-first in
-//    L2) and gathers x through the read-only path (evict-last in L2), then runs its
-//    segmented sum with one accumulate step per non-zero.  On GB300 the FP64 pipe issues
-//    about 2 lane-FMAs per clock per SM, so the FP64 form spends exactly one FMA per
-//    non-zero and amortises every other FP64 add over 32*S non-zeros;
+//  * bit flags and the slot -> row map come from tile_rows() (tile.cuh), the same code the
+//    parity kernel runs; the plain FP64 kernels build them one tile ahead, overlapped with
+//    the current tile's work;
+//  * each lane streams its own S consecutive non-zeros with 256-bit loads and gathers x
+//    through the read-only path, then runs its segmented sum with one accumulate step per
+//    non-zero: a branch per slot, or, when no lane has two row heads in a chunk (long rows),
+//    selects and one store per chunk.  On GB300 the FP64 pipe issues about 2 lane-FMAs per
+//    clock per SM, so the FP64 form spends exactly one FMA per non-zero and amortises every
+//    other FP64 add over 32*S non-zeros;
 //  * head-less lane partials are combined across lanes with a segmented suffix sum (a
 //    linear chain when the longest run of head-less lanes is short, a 5-step log scan
 //    otherwise), replacing the serial shared-memory walk of kernels_cuda.h:218-230;
 //  * rows are written at their true index: in a dirty tile the k-th row head maps to the
-//    k-th non-empty row of the span (listed by tile_flags), so there is no compacted y and
+//    k-th non-empty row of the span (listed by tile_rows), so there is no compacted y and
 //    no host fix-up;
 //  * a tile without any row head keeps its partial per lane across tiles and folds it only
 //    when the row ends (one butterfly per long row instead of one per tile);
