@@ -238,6 +238,15 @@ class Plan:
             raise SpmvError(rc, self.last_error)
         return sr.value, bool(oh.value)
 
+    def gather_path(self) -> tuple[int, int, bool]:
+        """(sampled non-zeros, those with a near column, whether x is gathered from L2 only)."""
+        sm, nr, l2 = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        rc = self._L.bhsp_plan_gather_path(self._p, ctypes.byref(sm), ctypes.byref(nr),
+                                           ctypes.byref(l2))
+        if rc != BHSPARSE_SUCCESS:
+            raise SpmvError(rc, self.last_error)
+        return sm.value, nr.value, bool(l2.value)
+
     @property
     def last_error(self) -> str:
         return self._L.bhsp_plan_last_error(self._p).decode()

@@ -87,6 +87,8 @@ struct bhsp_plan {
     uint32_t* err = nullptr;  // device error word
     int short_rows = 0;     // non-empty rows shorter than one chunk of a lane's slots
     bool one_head = false;  // the tile kernels take the one-head chunk form
+    int x_sampled = 0, x_near = 0;  // sampled non-zeros, those with a near column
+    bool x_l2 = false;              // the tile kernels gather x from L2 only
     int device = 0;
     std::string last_error;
 };
@@ -163,19 +165,27 @@ static int plan_build(bhsp_plan* p, cudaStream_t st) {
     PLAN_CUDA(p, cudaMalloc(&p->err, sizeof(uint32_t)));
     PLAN_CUDA(p, cudaMemsetAsync(p->err, 0, sizeof(uint32_t), st));
     PLAN_CUDA(p, launch_partition(p->row_ptr, p->m, p->nnz, tile, p->tile_ptr, st));
-    // the chunk form: rows shorter than the plain / mixed kernels' chunk width (scalar x
-    // entries: 4 slots at S = 8, else 8), counted on the device and read back once
+    // The kernel variant, from two counts made on the device and read back once:
+    //  - the chunk form: rows shorter than the plain / mixed kernels' chunk width (scalar x
+    //    entries: 4 slots at S = 8, else 8);
+    //  - the x gather path: the locality of the columns on about 2^20 sampled non-zeros.
     const int cw = p->cfg.seg == 8 ? 4 : 8;
-    uint32_t* count = nullptr;
-    uint32_t h = 0;
-    PLAN_CUDA(p, cudaMalloc(&count, sizeof(uint32_t)));
-    cudaError_t e = launch_short_rows(p->row_ptr, p->m, cw, count, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, count, sizeof h, cudaMemcpyDeviceToHost, st);
+    const int step = p->nnz > (1 << 20) ? p->nnz / (1 << 20) : 1;
+    uint32_t* counts = nullptr;
+    uint32_t h[3] = {0u, 0u, 0u};
+    PLAN_CUDA(p, cudaMalloc(&counts, 3 * sizeof(uint32_t)));
+    cudaError_t e = launch_short_rows(p->row_ptr, p->m, cw, counts, st);
+    if (e == cudaSuccess)
+        e = launch_x_locality(p->row_ptr, p->col, p->m, p->nnz, step, counts + 1, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, counts, sizeof h, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(count);
-    if (e != cudaSuccess) return cuda_fail(&p->last_error, e, "short-row count");
-    p->short_rows = (int)h;
-    p->one_head = one_head_pays(h, p->nnz, cw);
+    cudaFree(counts);
+    if (e != cudaSuccess) return cuda_fail(&p->last_error, e, "plan counts");
+    p->short_rows = (int)h[0];
+    p->one_head = one_head_pays(h[0], p->nnz, cw);
+    p->x_sampled = (int)h[1];
+    p->x_near = (int)h[2];
+    p->x_l2 = x_l2_pays(h[1], h[2]);
     return BHSPARSE_SUCCESS;
 }
 
@@ -201,6 +211,7 @@ static int plan_execute(bhsp_plan* p, const void* val, const void* x, void* y, c
             a.nnz = p->nnz;
             a.phase = phase;
             a.one_head = p->one_head;
+            a.x_l2 = p->x_l2;
             e = p->vt == BHSP_VALUE_F64 ? launch_plain_f64(a, p->cfg, st) : launch_plain_f32(a, p->cfg, st);
             break;
         }
@@ -221,6 +232,7 @@ static int plan_execute(bhsp_plan* p, const void* val, const void* x, void* y, c
             a.bf16 = p->vt == BHSP_VALUE_MIXED_BF16;
             a.phase = phase;
             a.one_head = p->one_head;
+            a.x_l2 = p->x_l2;
             e = launch_mixed(a, p->cfg, st);
             break;
         }
@@ -337,6 +349,14 @@ extern "C" int bhsp_plan_chunk_form(const bhsp_plan* p, int* short_rows, int* on
     if (!p) return BHSPARSE_INVALID_ARGUMENT;
     if (short_rows) *short_rows = p->short_rows;
     if (one_head) *one_head = p->one_head ? 1 : 0;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_plan_gather_path(const bhsp_plan* p, int* sampled, int* near, int* l2_only) {
+    if (!p) return BHSPARSE_INVALID_ARGUMENT;
+    if (sampled) *sampled = p->x_sampled;
+    if (near) *near = p->x_near;
+    if (l2_only) *l2_only = p->x_l2 ? 1 : 0;
     return BHSPARSE_SUCCESS;
 }
 

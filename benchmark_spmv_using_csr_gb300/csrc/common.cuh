@@ -197,6 +197,19 @@ __device__ __forceinline__ float ld_x(const float* p, uint64_t pol) {
 #endif
     return v;
 }
+// x gathers cached in L2 only (ld.global.cg): for matrices whose columns have no locality, where
+// L1 allocation buys almost no hits (the power-law matrix: 6.6 %) and costs L1 throughput.  x is
+// not written while a kernel runs, so the coherent path reads the same values.
+__device__ __forceinline__ double ld_x_l2(const double* p) {
+    double v;
+    asm volatile("ld.global.cg.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ float ld_x_l2(const float* p) {
+    float v;
+    asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
 
 // ---- warp helpers ----
 template <typename T>

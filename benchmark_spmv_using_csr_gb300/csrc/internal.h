@@ -23,6 +23,14 @@ cudaError_t launch_bitflags(const int* row_ptr, int m, int nnz, int seg, const u
                             uint32_t* words, cudaStream_t st);
 // *count = non-empty rows shorter than cw non-zeros (zeroed first)
 cudaError_t launch_short_rows(const int* row_ptr, int m, int cw, uint32_t* count, cudaStream_t st);
+// counts[0] = sampled non-zeros (every step-th), counts[1] = those whose column lies within 4 of
+// the previous entry of its row or of the entry at the same position of the previous row
+// (zeroed first)
+cudaError_t launch_x_locality(const int* row_ptr, const int* col, int m, int nnz, int step,
+                              uint32_t* counts, cudaStream_t st);
+// Whether the x gathers bypass L1: less than half of the sampled non-zeros have such a near
+// column (stencils and block matrices ~0.99, random columns <= 0.15).
+inline bool x_l2_pays(long long sampled, long long near) { return 2 * near < sampled; }
 // Whether the tile kernels take the one-head chunk form: the short rows can break at most 1/4
 // of the warp-chunks (32 lanes x cw slots).  Measured on rows of 27 non-zeros with a share of
 // 1-3-entry rows: the form still wins where they could break half of the chunks (1.00-1.06x),
@@ -48,6 +56,7 @@ struct PlainLaunch {
     int m, n, nnz;
     int phase;  // bit 0: tile kernel, bit 1: calibration kernel
     bool one_head = false;  // the plan's choice of the one-head chunk form
+    bool x_l2 = false;      // the plan's choice of L2-only x gathers
 };
 cudaError_t launch_plain_f64(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_plain_f32(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
@@ -68,6 +77,7 @@ struct MixedLaunch {
     bool bf16;
     int phase;  // bit 0: tile kernel, bit 1: calibration kernel
     bool one_head = false;  // the plan's choice of the one-head chunk form
+    bool x_l2 = false;      // the plan's choice of L2-only x gathers
 };
 cudaError_t launch_mixed(const MixedLaunch& a, const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_convert_from_f64(const double* src, void* dst, size_t n, bool to_bf16,

@@ -120,6 +120,60 @@ __global__ void k_short_rows(const int* __restrict__ row_ptr, int m, int cw,
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
 }
 
+// Locality of the columns for the x gathers, on every step-th non-zero: near when its column is
+// within 4 of the previous entry of its row, or of the entry at the same position of the
+// previous row (a stencil's neighbour rows reuse the same x lines).
+__global__ void k_x_locality(const int* __restrict__ row_ptr, const int* __restrict__ col, int m,
+                             int nnz, int step, uint32_t* __restrict__ counts) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    uint32_t seen = 0, near = 0;
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s * step < nnz;
+         s += stride) {
+        const int j = (int)(s * step);
+        // the row of non-zero j: the last r with row_ptr[r] <= j (rows 0..m-1)
+        int lo = 0, hi = m - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(row_ptr + mid) <= j)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const int r = lo;
+        const int start = __ldg(row_ptr + r);
+        const int c = __ldg(col + j);
+        bool is_near = false;
+        if (j > start) is_near = abs(c - __ldg(col + j - 1)) <= 4;
+        if (!is_near && r > 0) {
+            const int ps = __ldg(row_ptr + r - 1);
+            if (ps + (j - start) < start) is_near = abs(c - __ldg(col + ps + (j - start))) <= 4;
+        }
+        ++seen;
+        near += is_near ? 1u : 0u;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        seen += __shfl_xor_sync(SPMV_FULL_MASK, seen, d);
+        near += __shfl_xor_sync(SPMV_FULL_MASK, near, d);
+    }
+    if ((threadIdx.x & 31) == 0 && seen) {
+        atomicAdd(counts, seen);
+        atomicAdd(counts + 1, near);
+    }
+}
+
+cudaError_t launch_x_locality(const int* row_ptr, const int* col, int m, int nnz, int step,
+                              uint32_t* counts, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    if (m > 0 && nnz > 0 && step > 0) {
+        const long long samples = ((long long)nnz + step - 1) / step;
+        k_x_locality<<<grid_for(samples, 256, 152 * 8), 256, 0, st>>>(row_ptr, col, m, nnz, step,
+                                                                       counts);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_short_rows(const int* row_ptr, int m, int cw, uint32_t* count, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;

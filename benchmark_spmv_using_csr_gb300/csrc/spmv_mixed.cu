@@ -70,6 +70,7 @@ cudaError_t launch_mixed(const MixedLaunch& l, const TileConfig& cfg, cudaStream
         a.nnz = l.nnz;
         a.phase = l.phase;
         a.one_head = l.one_head;
+        a.x_l2 = l.x_l2;
         return launch_tiles_any(a, cfg, st);
     }
     TileArgs<PolMixed<float>> a;
@@ -87,6 +88,7 @@ cudaError_t launch_mixed(const MixedLaunch& l, const TileConfig& cfg, cudaStream
     a.nnz = l.nnz;
     a.phase = l.phase;
     a.one_head = l.one_head;
+    a.x_l2 = l.x_l2;
     return launch_tiles_any(a, cfg, st);
 }
 

@@ -69,6 +69,7 @@ static cudaError_t launch_plain_any(const PlainLaunch& l, const TileConfig& cfg,
     a.nnz = l.nnz;
     a.phase = l.phase;
     a.one_head = l.one_head;
+    a.x_l2 = l.x_l2;
     return launch_tiles_any<P>(a, cfg, st);
 }
 

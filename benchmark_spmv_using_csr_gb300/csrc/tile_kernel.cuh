@@ -59,6 +59,8 @@ struct TileArgs {
     // launcher choice, made at plan time: the kernel specialised for the one-head chunk form
     // (few rows shorter than a chunk, so that most chunks take it)
     bool one_head = false;
+    // launcher choice, made at plan time: x gathers from L2 only (columns without locality)
+    bool x_l2 = false;
 };
 
 // ---- shuffles for the accumulator types ----
@@ -92,18 +94,26 @@ __host__ __device__ constexpr int chunk_width() {
     return sizeof(XT) > 16 ? 2 : (S == 8 || sizeof(XT) > 8) ? 4 : 8;
 }
 
-template <int CW, typename XT>
+// one x entry: through L1 (read-only path), or from L2 only (XL2)
+template <bool XL2, typename XT>
+__device__ __forceinline__ XT ld_x_sel(const XT* p, uint64_t pol) {
+    if constexpr (XL2)
+        return ld_x_l2(p);
+    else
+        return ld_x(p, pol);
+}
+template <bool XL2, int CW, typename XT>
 __device__ __forceinline__ void gather_cw(const XT* __restrict__ x, const int (&c)[CW], uint64_t pol,
                                           XT (&xv)[CW]) {
 #pragma unroll
-    for (int i = 0; i < CW; ++i) xv[i] = c[i] >= 0 ? ld_x(x + c[i], pol) : XT(0);
+    for (int i = 0; i < CW; ++i) xv[i] = c[i] >= 0 ? ld_x_sel<XL2>(x + c[i], pol) : XT(0);
 }
 // x entries of a chunk of a full tile, which has no padding slot (column -1) to test
-template <int CW, typename XT>
+template <bool XL2, int CW, typename XT>
 __device__ __forceinline__ void gather_cw_full(const XT* __restrict__ x, const int (&c)[CW],
                                                uint64_t pol, XT (&xv)[CW]) {
 #pragma unroll
-    for (int i = 0; i < CW; ++i) xv[i] = ld_x(x + c[i], pol);
+    for (int i = 0; i < CW; ++i) xv[i] = ld_x_sel<XL2>(x + c[i], pol);
 }
 
 template <typename YT>
@@ -327,7 +337,7 @@ __device__ __forceinline__ void chunk_segments(bool one_head, uint32_t cb, int k
 // multiplied, the values of chunk g+1 and the column indices of chunk g+2 are in flight and the
 // x gathers of chunk g+1 are issued; the bit flags' row_ptr entries and tile_ptr are fetched
 // one tile ahead.
-template <class P, int S, bool OH = false, bool MID = false>
+template <class P, int S, bool OH = false, bool MID = false, bool XL2 = false>
 __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, int tpw, int ntiles,
                                             uint32_t* const s_words_w, int* const rowof) {
     using Acc = typename P::Acc;
@@ -365,7 +375,7 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
             load_vals_tile8(a, t_begin, lane, pol_s, valA, valC);
         else
             load_vals<P, S, CW>(a, t_begin, 0, lane, pol_s, valA);
-        gather_cw(a.x, col0, pol_x, xA);
+        gather_cw<XL2>(a.x, col0, pol_x, xA);
         const int t1 = t_begin + (NC > 1 ? 0 : 1);
         const int c1 = NC > 1 ? 1 : 0;
         if (t1 < t_end) load_cols<P, S, CW>(a, t1, c1, lane, pol_s, colA);
@@ -490,9 +500,9 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
                 // the one-head kernels gather a full tile's x without the padding test (1 %
                 // on the 27-point stencil; the per-slot kernels measured no gain from it)
                 if (one_head && (long long)(t1 + 1) * TILE <= a.nnz)
-                    gather_cw_full(a.x, colA, pol_x, xB);
+                    gather_cw_full<XL2>(a.x, colA, pol_x, xB);
                 else
-                    gather_cw(a.x, colA, pol_x, xB);
+                    gather_cw<XL2>(a.x, colA, pol_x, xB);
             }
             // multiply chunk g (its row-head bits: slot c*CW in bit CW-1)
             const uint32_t cb = (w >> (32 - (c + 1) * CW)) & ((1u << CW) - 1u);
@@ -567,7 +577,7 @@ struct MinBlocks {
 };
 
 // One warp = one worker, worker = global warp index (static schedule).
-template <class P, int S, int WARPS, bool OH>
+template <class P, int S, int WARPS, bool OH, bool XL2>
 __global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
     k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
     // Plain FP64 with the one-head form (long rows) keeps two slot -> row maps per warp where
@@ -583,7 +593,7 @@ __global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
     const int warp = threadIdx.x >> 5;
     const int worker = blockIdx.x * WARPS + warp;
     if (worker >= nworkers) return;
-    tile_worker<P, S, OH, MID>(a, worker, tpw, ntiles, s_words[warp], s_rowof[warp]);
+    tile_worker<P, S, OH, MID, XL2>(a, worker, tpw, ntiles, s_words[warp], s_rowof[warp]);
 }
 
 // Persistent schedule: a grid sized to the GPU's resident capacity; each warp takes the next
@@ -735,12 +745,17 @@ cudaError_t launch_tiles_t(const TileArgs<P>& a, int tpw, int nworkers, int ntil
     if (nworkers > 0 && (a.phase & 1)) {
         const int blocks = (nworkers + WARPS - 1) / WARPS;
         if constexpr (sizeof(typename P::Acc) <= 8) {  // scalar accumulators: either form
-            if (a.one_head)
-                k_tiles<P, S, WARPS, true><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+            // chunk form x gather path, both fixed by the plan
+            if (a.one_head && a.x_l2)
+                k_tiles<P, S, WARPS, true, true><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+            else if (a.one_head)
+                k_tiles<P, S, WARPS, true, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+            else if (a.x_l2)
+                k_tiles<P, S, WARPS, false, true><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
             else
-                k_tiles<P, S, WARPS, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+                k_tiles<P, S, WARPS, false, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
         } else {
-            k_tiles<P, S, WARPS, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+            k_tiles<P, S, WARPS, false, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
         }
     }
     if (a.phase & 2) {

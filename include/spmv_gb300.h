@@ -143,6 +143,11 @@ int bhsp_plan_tiles(const bhsp_plan* p, const uint32_t** d_tile_ptr, int* ntiles
  * non-empty rows shorter than one chunk of a lane's slots (4 at seg 8, else 8), *one_head = 1
  * when they are few enough (at most 1/4 of the warp-chunks) for the branch-free one-head form. */
 int bhsp_plan_chunk_form(const bhsp_plan* p, int* short_rows, int* one_head);
+/* The x gather path the plan's tile kernels take, fixed when the plan is built: of *sampled
+ * non-zeros (every nnz / 2^20-th), *near have a column within 4 of the previous entry of their
+ * row or of the same-position entry of the previous row; *l2_only = 1 (x gathered from L2
+ * only, ld.global.cg) when fewer than half do, else x goes through L1. */
+int bhsp_plan_gather_path(const bhsp_plan* p, int* sampled, int* near, int* l2_only);
 const char* bhsp_plan_last_error(const bhsp_plan* p);
 void bhsp_plan_destroy(bhsp_plan* p);
 

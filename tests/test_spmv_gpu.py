@@ -271,6 +271,43 @@ def test_one_head_chunk_form_decision(cuda_ok, seg):
     assert got_short == int(np.count_nonzero((lens > 0) & (lens < cw))) and on
 
 
+def _x_locality(rp, col):
+    """numpy restatement of the plan's sample: every max(1, nnz // 2^20)-th non-zero, near when
+    its column is within 4 of the previous entry of its row or of the same-position entry of
+    the previous row."""
+    nnz = int(rp[-1])
+    step = nnz // (1 << 20) if nnz > (1 << 20) else 1
+    j = np.arange(0, nnz, step, dtype=np.int64)
+    r = np.searchsorted(rp.astype(np.int64), j, side="right") - 1
+    start = rp[r].astype(np.int64)
+    c = col[j].astype(np.int64)
+    near = np.zeros(j.size, bool)
+    inrow = j > start
+    near[inrow] = np.abs(c[inrow] - col[j[inrow] - 1]) <= 4
+    ok = (~near) & (r > 0)
+    ps = np.where(ok, rp[np.maximum(r - 1, 0)], 0).astype(np.int64)
+    ok &= ps + (j - start) < start
+    near[ok] = np.abs(c[ok] - col[ps[ok] + (j[ok] - start[ok])]) <= 4
+    return j.size, int(near.sum())
+
+
+def test_gather_path_decision(cuda_ok):
+    """The plan samples the columns' locality and gathers x from L2 only (ld.global.cg) when
+    fewer than half of the sampled non-zeros have a near column: off for stencils and block
+    matrices, on for random columns."""
+    import torch
+    cases = ((gen.stencil3d(24, 20, 17, seed=3), False), (gen.stencil2d(97, 131, seed=2), False),
+             (gen.blockdiag(9000, 9000, 32), False), (gen.powerlaw(30000, seed=4), True),
+             (gen.density(20000, 20000, 1e-3, seed=6), True))
+    for a, l2 in cases:
+        p = sp.Plan(sp.VALUE_F64, a.m, a.n, torch.from_numpy(a.row_ptr).cuda(),
+                    torch.from_numpy(a.col).cuda())
+        sampled, near, got = p.gather_path()
+        p.close()
+        assert (sampled, near) == _x_locality(a.row_ptr, a.col)
+        assert got == (2 * near < sampled) == l2
+
+
 @pytest.mark.parametrize("cfg", CONFIGS)
 def test_one_head_form_with_fallback_chunks_bit_exact(cuda_ok, cfg):
     """Long rows with sparse short and empty rows: most chunks take the one-head form, the
