@@ -67,6 +67,15 @@ def test_config_validation_without_gpu():
     s.close()
 
 
+def test_plan_queries_reject_a_null_plan():
+    L = lib()
+    n = ctypes.c_int()
+    assert L.bhsp_plan_chunk_form(None, ctypes.byref(n), ctypes.byref(n)) == sp.BHSPARSE_INVALID_ARGUMENT
+    assert L.bhsp_plan_gather_path(None, ctypes.byref(n), ctypes.byref(n),
+                                   ctypes.byref(n)) == sp.BHSPARSE_INVALID_ARGUMENT
+    assert L.bhsp_plan_tiles(None, None, None, None) == sp.BHSPARSE_INVALID_ARGUMENT
+
+
 def test_run_before_prepare_is_an_error():
     s = sp.BhsparseSpmvCuda(sp.VALUE_F32)
     assert s.run_benchmark() == sp.BHSPARSE_NOT_PREPARED
