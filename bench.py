@@ -156,11 +156,38 @@ class ClockSampler:
                 "power_w_max": max((num(r[3]) or 0) for r in loaded), "reasons": sorted(reasons)}
 
 
-def make_workload(name: str):
+def make_workload(name: str, cpu_only: bool = False):
+    """The seeded workload and its x.  cpu_only: take the generators from oracle/'s own build of
+    the generator source instead of the GPU library (the reference arm loads no product code)."""
     from benchmark_spmv_using_csr_gb300 import gen
+    if cpu_only:
+        import oracle
+        gen.use_library(oracle.gen_library_path())
     a = gen.WORKLOADS[name]()
     x = gen.uniform(a.n, 7)
     return a, x
+
+
+def l2_text(a) -> str:
+    mb = alg_bytes(a.m, a.n, a.nnz, 8, 8, 8) / 1e6
+    size = (f"inputs larger than L2 ({mb:.0f} MB of algorithmic bytes against a 129 MB L2)"
+            if mb > 129 else f"inputs of {mb:.1f} MB, which fit in the 129 MB L2")
+    return size + "; the GPU arm writes 256 MiB before every timed step to flush L2"
+
+
+def workload_config(name: str, a, x) -> dict:
+    """The `config` object both arms print: the workload, its sizes, its algorithmic bytes and a
+    CRC-32 of its arrays (row_ptr, col_idx, val, x), which shows that both arms ran the same
+    matrix."""
+    import zlib
+
+    import numpy as np
+    crc = 0
+    for arr in (a.row_ptr, a.col, a.val, x):
+        crc = zlib.crc32(np.ascontiguousarray(arr).view(np.uint8), crc)
+    return {"workload": name, "description": WORKLOAD_TEXT[name], "m": a.m, "n": a.n,
+            "nnz": a.nnz, "bytes_per_step": alg_bytes(a.m, a.n, a.nnz, 8, 8, 8),
+            "matrix_crc32": f"{crc:08x}", "l2": l2_text(a)}
 
 
 def dist_env():
@@ -192,21 +219,38 @@ def whole_job_gbs(world: int, bytes_per_step: int, steps: int, seconds: float) -
 # reference arm: the reference's CPU path (port) on all host cores
 # ---------------------------------------------------------------------------------------
 def run_reference(args) -> None:
+    """The reference's CPU path on all host cores: its own OpenMP CSR loop (spmv_cuda/main.cu:
+    377-393) compiled from its sources into oracle/_ref/libref.so where that was built, else the
+    C port in oracle/.  Rank 0 only; no GPU library is loaded."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
     import numpy as np
     import oracle
-    a, x = make_workload(args.workload)
+    a, x = make_workload(args.workload, cpu_only=True)
     threads = os.cpu_count() or 1
     B = alg_bytes(a.m, a.n, a.nnz, 8, 8, 8)
     y = np.zeros(a.m)
+    if oracle.ref_lib() is not None:
+        kind = "reference"
+        what = ("the reference's own OpenMP CSR loop (spmv_cuda/main.cu:377-393), compiled from "
+                "its source by oracle/Makefile (oracle/_ref/libref.so)")
+
+        def step():
+            oracle.ref_omp(a.row_ptr, a.col, a.val, x, threads, runs=1, y=y)
+    else:
+        kind = "port"
+        what = ("the C port of the reference's OpenMP CSR loop (spmv_cuda/main.cu:377-393) in "
+                "oracle/; the reference's own loop was not compiled on this host")
+
+        def step():
+            oracle.csr_omp(a.row_ptr, a.col, a.val, x, threads, y=y)
     for _ in range(args.warmup):
-        oracle.csr_omp(a.row_ptr, a.col, a.val, x, threads, y=y)
+        step()
     ts = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle.csr_omp(a.row_ptr, a.col, a.val, x, threads, y=y)
+        step()
         ts.append(time.perf_counter() - t0)
     sec = sum(ts)
     value = B * args.steps / sec / 1e9
@@ -215,14 +259,10 @@ def run_reference(args) -> None:
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * sec / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, "description": WORKLOAD_TEXT[args.workload],
-                   "m": a.m, "n": a.n, "nnz": a.nnz, "bytes_per_step": B},
-        "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads,
-                         "kind": "port",
-                         "sample": "whole matrix per step; OpenMP CSR loop of spmv_cuda/main.cu:"
-                                   "377-393 (C port in oracle/), all host threads; the reference's "
-                                   "own build (sm_32, CUDA-samples headers, removed cuSPARSE "
-                                   "calls) does not compile with CUDA 13"},
+        "config": workload_config(args.workload, a, x),
+        "parallelism": f"{threads} host threads (rank 0 only)",
+        "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"one whole-matrix pass per step, {args.steps} steps: {what}"},
         "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -383,13 +423,11 @@ def run_ours(args) -> None:
             "ms_per_step": round(statistics.mean(step_ms), 5), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded generators; no dataset)",
-            "config": {"workload": args.workload, "description": WORKLOAD_TEXT[args.workload],
-                       "m": a.m, "n": a.n, "nnz": a.nnz, "bytes_per_step": B,
-                       "reference_formula_bytes": reference_formula_bytes(a.m, a.nnz, 8),
-                       "tile": {"nnz_per_lane": seg, "tiles_per_worker": tpw,
-                                "warps_per_cta": warps, "tma_stages": stages},
-                       "l2": "256 MiB flush write before every timed step; A (0.7 GB) > L2",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "config": workload_config(args.workload, a, x),
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "reference_formula_bytes": reference_formula_bytes(a.m, a.nnz, 8),
+            "schedule": {"nnz_per_lane": seg, "tiles_per_worker": tpw, "warps_per_cta": warps,
+                         "tma_stages": stages},
             "pct_peak": round(100.0 * value / peak, 2),
             "rel_error": {"componentwise_vs_fp64_dot2": rel_err, "tolerance": 1e-12},
             "phases_ms": {"tile_kernel": round(kmean, 5),

@@ -56,8 +56,9 @@ def _compile(nvcc: str, src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if _stale(obj, [src] + _headers()):
         cmd = [nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj]
-        if src.endswith(".cpp"):
-            cmd = [nvcc, "-x", "c++"] + NVCC_FLAGS[len(ARCH):] + ["-c", src, "-o", obj]
+        if src.endswith(".cpp"):  # host-only code; no FMA contraction on any host CPU
+            cmd = [nvcc, "-x", "c++"] + NVCC_FLAGS[len(ARCH):] + ["-Xcompiler", "-ffp-contract=off",
+                                                                 "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -426,10 +426,11 @@ struct bhsp_spmv {
     cudaStream_t stream = nullptr;  // stream used by run_benchmark / set_x / get_y
     std::string last_error;
     std::string device_name;
-    // bhsp_run_stream: a second x / y pair (the first is d_x / d_y), an upload, a compute and a
-    // download stream, and per-buffer events; created on first use
-    void* d_x1 = nullptr;
-    void* d_y1 = nullptr;
+    // bhsp_run_stream: two x / y buffer pairs of its own (the handle's d_x / d_y are left as they
+    // were), an upload, a compute and a download stream, and per-buffer events; created on first
+    // use
+    void* d_xs[2] = {nullptr, nullptr};
+    void* d_ys[2] = {nullptr, nullptr};
     cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
     cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr},
                 ev_out[2] = {nullptr, nullptr};
@@ -496,9 +497,11 @@ extern "C" int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tpw, int* warp
 }
 
 static void stream_release(bhsp_spmv* h) {
-    cudaFree(h->d_x1);
-    cudaFree(h->d_y1);
-    h->d_x1 = h->d_y1 = nullptr;
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(h->d_xs[i]);
+        cudaFree(h->d_ys[i]);
+        h->d_xs[i] = h->d_ys[i] = nullptr;
+    }
     for (int i = 0; i < 2; ++i) {
         if (h->ev_in[i]) cudaEventDestroy(h->ev_in[i]);
         if (h->ev_comp[i]) cudaEventDestroy(h->ev_comp[i]);
@@ -662,8 +665,10 @@ extern "C" int bhsp_get_y(bhsp_spmv* h) {
 static int stream_setup(bhsp_spmv* h) {
     if (h->s_comp) return BHSPARSE_SUCCESS;
     const size_t vb = vec_bytes(h->vt);
-    H_CUDA(h, cudaMalloc(&h->d_x1, vb * (size_t)(h->n > 0 ? h->n : 1)));
-    H_CUDA(h, cudaMalloc(&h->d_y1, vb * (size_t)(h->m > 0 ? h->m : 1)));
+    for (int i = 0; i < 2; ++i) {
+        H_CUDA(h, cudaMalloc(&h->d_xs[i], vb * (size_t)(h->n > 0 ? h->n : 1)));
+        H_CUDA(h, cudaMalloc(&h->d_ys[i], vb * (size_t)(h->m > 0 ? h->m : 1)));
+    }
     H_CUDA(h, cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking));
     H_CUDA(h, cudaStreamCreateWithFlags(&h->s_comp, cudaStreamNonBlocking));
     H_CUDA(h, cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking));
@@ -688,41 +693,57 @@ extern "C" int bhsp_run_stream(bhsp_spmv* h, int count, const void* const* x_hos
             return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "null host vector");
     H_CUDA(h, cudaSetDevice(h->device));
     int rc = stream_setup(h);
-    if (rc) return rc;
+    if (rc) {
+        stream_release(h);  // a partial set-up is not kept
+        return rc;
+    }
     H_CUDA(h, cudaStreamSynchronize(h->stream));  // the handle's own work comes first
+    // every failure below waits for all three streams, so that no copy or kernel of this call
+    // is still running when it returns
+    auto drain = [&](int code) {
+        cudaStreamSynchronize(h->s_in);
+        cudaStreamSynchronize(h->s_comp);
+        cudaStreamSynchronize(h->s_out);
+        return code;
+    };
+#define S_CUDA(call)                                                                      \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) return drain(cuda_fail(&h->last_error, e_, #call));        \
+    } while (0)
     const size_t vb = vec_bytes(h->vt);
-    void* X[2] = {h->d_x, h->d_x1};
-    void* Y[2] = {h->d_y, h->d_y1};
+    void* const* X = h->d_xs;
+    void* const* Y = h->d_ys;
     for (int i = 0; i < count; ++i) {
         const int b = i & 1;
         // x_i into X[b] once the SpMV of i-2 has read it
-        if (i >= 2) H_CUDA(h, cudaStreamWaitEvent(h->s_in, h->ev_comp[b], 0));
+        if (i >= 2) S_CUDA(cudaStreamWaitEvent(h->s_in, h->ev_comp[b], 0));
         if (h->n > 0)
-            H_CUDA(h, cudaMemcpyAsync(X[b], x_host[i], vb * (size_t)h->n, cudaMemcpyHostToDevice,
-                                      h->s_in));
-        H_CUDA(h, cudaEventRecord(h->ev_in[b], h->s_in));
+            S_CUDA(cudaMemcpyAsync(X[b], x_host[i], vb * (size_t)h->n, cudaMemcpyHostToDevice,
+                                   h->s_in));
+        S_CUDA(cudaEventRecord(h->ev_in[b], h->s_in));
         // y_i = A x_i once x_i has landed and y_{i-2} has left Y[b]
-        H_CUDA(h, cudaStreamWaitEvent(h->s_comp, h->ev_in[b], 0));
-        if (i >= 2) H_CUDA(h, cudaStreamWaitEvent(h->s_comp, h->ev_out[b], 0));
+        S_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_in[b], 0));
+        if (i >= 2) S_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_out[b], 0));
         rc = bhsp_plan_execute(h->plan, h->d_val, X[b], Y[b], h->s_comp);
         if (rc) {
             h->last_error = h->plan->last_error;
-            cudaStreamSynchronize(h->s_in);
-            cudaStreamSynchronize(h->s_comp);
-            cudaStreamSynchronize(h->s_out);
-            return rc;
+            return drain(rc);
         }
-        H_CUDA(h, cudaEventRecord(h->ev_comp[b], h->s_comp));
+        S_CUDA(cudaEventRecord(h->ev_comp[b], h->s_comp));
         // y_i to the host
-        H_CUDA(h, cudaStreamWaitEvent(h->s_out, h->ev_comp[b], 0));
+        S_CUDA(cudaStreamWaitEvent(h->s_out, h->ev_comp[b], 0));
         if (h->m > 0)
-            H_CUDA(h, cudaMemcpyAsync(y_host[i], Y[b], vb * (size_t)h->m, cudaMemcpyDeviceToHost,
-                                      h->s_out));
-        H_CUDA(h, cudaEventRecord(h->ev_out[b], h->s_out));
+            S_CUDA(cudaMemcpyAsync(y_host[i], Y[b], vb * (size_t)h->m, cudaMemcpyDeviceToHost,
+                                   h->s_out));
+        S_CUDA(cudaEventRecord(h->ev_out[b], h->s_out));
     }
-    H_CUDA(h, cudaStreamSynchronize(h->s_in));
-    H_CUDA(h, cudaStreamSynchronize(h->s_comp));
-    H_CUDA(h, cudaStreamSynchronize(h->s_out));
+#undef S_CUDA
+    cudaError_t e = cudaStreamSynchronize(h->s_in);
+    const cudaError_t e2 = cudaStreamSynchronize(h->s_comp);
+    const cudaError_t e3 = cudaStreamSynchronize(h->s_out);
+    if (e == cudaSuccess) e = e2 != cudaSuccess ? e2 : e3;
+    if (e != cudaSuccess) return cuda_fail(&h->last_error, e, "bhsp_run_stream");
     rc = plan_check(h->plan, h->s_comp);
     if (rc) h->last_error = h->plan->last_error;
     return rc;
@@ -763,5 +784,6 @@ extern "C" size_t bhsp_device_bytes(const bhsp_spmv* h) {
     size_t b = sizeof(int) * ((size_t)h->m + 1) + sizeof(int) * (size_t)h->nnz +
                val_bytes(h->vt) * (size_t)h->nnz + vec_bytes(h->vt) * ((size_t)h->n + h->m);
     if (h->plan) b += sizeof(uint32_t) * ((size_t)h->plan->ntiles + 1) + 12 * (size_t)h->plan->nworkers;
+    if (h->d_xs[0]) b += 2 * vec_bytes(h->vt) * ((size_t)h->n + h->m);  // bhsp_run_stream's pairs
     return b;
 }

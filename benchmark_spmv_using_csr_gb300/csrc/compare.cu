@@ -8,6 +8,7 @@
 
 #include "../../include/spmv_compare.h"
 #include "../../include/spmv_gb300.h"
+#include "internal.h"
 
 namespace {
 
@@ -50,8 +51,7 @@ cudaError_t launch_vector(int m, const int* rp, const int* col, const VT* val, c
                           int tpv, cudaStream_t st) {
     if (m <= 0) return cudaSuccess;
     const int threads = 256;
-    long long blocks = ((long long)m * tpv + threads - 1) / threads;
-    if (blocks > 152 * 16) blocks = 152 * 16;  // grid-stride beyond 16 blocks per SM
+    const long long blocks = spmv::grid_for((long long)m * tpv, threads, 16);  // grid-stride beyond 16 blocks per SM
     switch (tpv) {
         case 2: k_csr_vector<VT, 2><<<(int)blocks, threads, 0, st>>>(m, rp, col, val, x, y); break;
         case 4: k_csr_vector<VT, 4><<<(int)blocks, threads, 0, st>>>(m, rp, col, val, x, y); break;

@@ -7,6 +7,12 @@ namespace spmv {
 
 inline int num_tiles(int nnz, int tile) { return (int)(((long long)nnz + tile - 1) / tile); }
 
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount, looked up
+// once per device; 152 on a GB300).  Grid-stride launchers cap their grids at a multiple of it.
+int device_sm_count();
+// min(ceil(work / threads), cap_per_sm * SMs), at least 1: the grid of a grid-stride launch
+int grid_for(long long work, int threads, int cap_per_sm);
+
 // Schedule of the plain / mixed tile kernels: S non-zeros per lane (tile = 32*S), a worker
 // (one warp) walks `tiles_per_worker` consecutive tiles, `warps_per_cta` workers per CTA.
 struct TileConfig {

@@ -1,5 +1,7 @@
 // partition.cu -- tile_ptr construction (binary-search partition + dirty bits), the
 // bit-flag parity kernel, and the CSR validation pass run before a matrix is accepted.
+#include <atomic>
+
 #include "internal.h"
 #include "tile.cuh"
 
@@ -70,20 +72,37 @@ __global__ void k_validate(const int* __restrict__ row_ptr, const int* __restric
     }
 }
 
-static int grid_for(long long work, int threads, int cap) {
+
+int device_sm_count() {
+    static std::atomic<int> cache[64];  // zero: not looked up yet
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+    if (dev < 64) {
+        const int c = cache[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+        return 1;
+    if (dev < 64) cache[dev].store(sms, std::memory_order_relaxed);
+    return sms;
+}
+
+int grid_for(long long work, int threads, int cap_per_sm) {
     long long g = (work + threads - 1) / threads;
-    if (g < 1) g = 1;
+    const long long cap = (long long)cap_per_sm * device_sm_count();
     if (g > cap) g = cap;
+    if (g < 1) g = 1;
     return (int)g;
 }
 
 cudaError_t launch_partition(const int* row_ptr, int m, int nnz, int tile, uint32_t* tile_ptr,
                              cudaStream_t st) {
     const int nt = num_tiles(nnz, tile);
-    k_tile_rows<<<grid_for(nt + 1, 256, 1 << 20), 256, 0, st>>>(row_ptr, m, nnz, tile, nt,
+    k_tile_rows<<<(unsigned)(((long long)nt + 1 + 255) / 256), 256, 0, st>>>(row_ptr, m, nnz, tile, nt,
                                                                 tile_ptr);
     if (m > 0 && nt > 0)
-        k_mark_dirty<<<grid_for(m, 256, 152 * 16), 256, 0, st>>>(row_ptr, m, tile, nt, tile_ptr);
+        k_mark_dirty<<<grid_for(m, 256, 16), 256, 0, st>>>(row_ptr, m, tile, nt, tile_ptr);
     return cudaGetLastError();
 }
 
@@ -168,7 +187,7 @@ cudaError_t launch_x_locality(const int* row_ptr, const int* col, int m, int nnz
     if (e != cudaSuccess) return e;
     if (m > 0 && nnz > 0 && step > 0) {
         const long long samples = ((long long)nnz + step - 1) / step;
-        k_x_locality<<<grid_for(samples, 256, 152 * 8), 256, 0, st>>>(row_ptr, col, m, nnz, step,
+        k_x_locality<<<grid_for(samples, 256, 8), 256, 0, st>>>(row_ptr, col, m, nnz, step,
                                                                        counts);
     }
     return cudaGetLastError();
@@ -177,14 +196,14 @@ cudaError_t launch_x_locality(const int* row_ptr, const int* col, int m, int nnz
 cudaError_t launch_short_rows(const int* row_ptr, int m, int cw, uint32_t* count, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    if (m > 0) k_short_rows<<<grid_for(m, 256, 152 * 8), 256, 0, st>>>(row_ptr, m, cw, count);
+    if (m > 0) k_short_rows<<<grid_for(m, 256, 8), 256, 0, st>>>(row_ptr, m, cw, count);
     return cudaGetLastError();
 }
 
 cudaError_t launch_validate(const int* row_ptr, const int* col, int m, int n, int nnz,
                             uint32_t* bad, cudaStream_t st) {
     long long work = (long long)(m > nnz ? m : nnz);
-    k_validate<<<grid_for(work, 256, 152 * 8), 256, 0, st>>>(row_ptr, col, m, n, nnz, bad);
+    k_validate<<<grid_for(work, 256, 8), 256, 0, st>>>(row_ptr, col, m, n, nnz, bad);
     return cudaGetLastError();
 }
 

@@ -186,9 +186,7 @@ static cudaError_t enqueue_batched(const TileArgs<PolMixedK<K>>& a, int tpw, int
     if (nworkers > 0)
         persistent_kernel<K, S, WARPS>()<<<grid, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles,
                                                                      ticket);
-    int cb = (nworkers + 255) / 256;
-    if (cb < 1) cb = 1;
-    if (cb > 152 * 8) cb = 152 * 8;
+    const int cb = grid_for(nworkers, 256, 8);
     k_calibrate<PolMixedK<K>><<<cb, 256, 0, st>>>(a.rec_row, a.rec_val, nworkers, a.y, a.tile_ptr,
                                                   a.m, a.err);
     return cudaGetLastError();

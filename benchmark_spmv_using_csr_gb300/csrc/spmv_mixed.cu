@@ -116,15 +116,13 @@ __global__ void k_to_f64(const float* __restrict__ src, double* __restrict__ dst
 cudaError_t launch_convert_from_f64(const double* src, void* dst, size_t n, bool to_bf16,
                                     cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    size_t g = (n + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
+    const int g = grid_for((long long)n, 256, 16);
     k_from_f64<<<(unsigned)g, 256, 0, st>>>(src, dst, n, to_bf16);
     return cudaGetLastError();
 }
 cudaError_t launch_convert_to_f64(const float* src, double* dst, size_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    size_t g = (n + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
+    const int g = grid_for((long long)n, 256, 16);
     k_to_f64<<<(unsigned)g, 256, 0, st>>>(src, dst, n);
     return cudaGetLastError();
 }

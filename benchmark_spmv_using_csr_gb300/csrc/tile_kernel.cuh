@@ -722,9 +722,7 @@ __global__ void k_calibrate(const int* __restrict__ rec_row,
 // device (griddepcontrol.wait), which hides the launch gap between the two.
 template <class P>
 cudaError_t launch_calibrate(const TileArgs<P>& a, int nworkers, cudaStream_t st) {
-    int cb = (nworkers + 255) / 256;
-    if (cb < 1) cb = 1;
-    if (cb > 152 * 8) cb = 152 * 8;
+    const int cb = grid_for(nworkers, 256, 8);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cb);
     cfg.blockDim = dim3(256);

@@ -158,8 +158,7 @@ extern "C" int bhsp_row_features(const int* d_row_ptr, int m, int n, float* feat
     int rc = BHSPARSE_SUCCESS;
     if (cudaMemsetAsync(acc, 0, sizeof h, st) != cudaSuccess) rc = BHSPARSE_CUDA_ERROR;
     if (!rc && m > 0) {
-        int blocks = (m + 255) / 256;
-        if (blocks > 152 * 8) blocks = 152 * 8;
+        const int blocks = spmv::grid_for(m, 256, 8);
         spmv::k_row_features<<<blocks, 256, 0, st>>>(d_row_ptr, m, acc);
         if (cudaGetLastError() != cudaSuccess) rc = BHSPARSE_CUDA_ERROR;
     }

@@ -18,7 +18,28 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import lib
+from ._lib import SIGNATURES, lib
+
+_gen_override = None
+
+
+def use_library(path: str) -> None:
+    """Take the generators from another build of csrc/gen.cpp (a shared library exporting the
+    bhsp_gen_* functions of include/spmv_gen.h), so that a CPU-only process can build the same
+    seeded matrices without loading the GPU library."""
+    global _gen_override
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        if name.startswith("bhsp_gen_"):
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+    _gen_override = L
+
+
+def _lib():
+    return _gen_override if _gen_override is not None else lib()
+
 
 POWERLAW_ALPHA = 2.1
 POWERLAW_XMIN = 1.98
@@ -52,25 +73,25 @@ def _check(rc, what):
 
 def uniform(count: int, seed: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
     out = np.empty(max(count, 0), np.float64)
-    _check(lib().bhsp_gen_uniform(int(count), int(seed), float(lo), float(hi), _p(out)), "uniform")
+    _check(_lib().bhsp_gen_uniform(int(count), int(seed), float(lo), float(hi), _p(out)), "uniform")
     return out
 
 
 def uniform_int(count: int, seed: int, modulus: int = 10) -> np.ndarray:
     """Integer-valued doubles in [0, modulus): the reference's rand()%10 data, seeded."""
     out = np.empty(max(count, 0), np.float64)
-    _check(lib().bhsp_gen_uniform_int(int(count), int(seed), int(modulus), _p(out)), "uniform_int")
+    _check(_lib().bhsp_gen_uniform_int(int(count), int(seed), int(modulus), _p(out)), "uniform_int")
     return out
 
 
 def stencil2d(nx: int, ny: int | None = None, noise: float = 1e-3, seed: int = 1) -> CSR:
     ny = nx if ny is None else ny
-    nnz = _check(lib().bhsp_gen_stencil2d_nnz(nx, ny), "stencil2d_nnz")
+    nnz = _check(_lib().bhsp_gen_stencil2d_nnz(nx, ny), "stencil2d_nnz")
     m = nx * ny
     rp = np.empty(m + 1, np.int32)
     col = np.empty(nnz, np.int32)
     val = np.empty(nnz, np.float64)
-    _check(lib().bhsp_gen_stencil2d(nx, ny, float(noise), int(seed), _p(rp), _p(col), _p(val)),
+    _check(_lib().bhsp_gen_stencil2d(nx, ny, float(noise), int(seed), _p(rp), _p(col), _p(val)),
            "stencil2d")
     return CSR(m, m, rp, col, val, f"stencil5_{nx}x{ny}")
 
@@ -79,12 +100,12 @@ def stencil3d(nx: int, ny: int | None = None, nz: int | None = None, noise: floa
               seed: int = 1) -> CSR:
     ny = nx if ny is None else ny
     nz = nx if nz is None else nz
-    nnz = _check(lib().bhsp_gen_stencil3d_nnz(nx, ny, nz), "stencil3d_nnz")
+    nnz = _check(_lib().bhsp_gen_stencil3d_nnz(nx, ny, nz), "stencil3d_nnz")
     m = nx * ny * nz
     rp = np.empty(m + 1, np.int32)
     col = np.empty(nnz, np.int32)
     val = np.empty(nnz, np.float64)
-    _check(lib().bhsp_gen_stencil3d(nx, ny, nz, float(noise), int(seed), _p(rp), _p(col), _p(val)),
+    _check(_lib().bhsp_gen_stencil3d(nx, ny, nz, float(noise), int(seed), _p(rp), _p(col), _p(val)),
            "stencil3d")
     return CSR(m, m, rp, col, val, f"stencil27_{nx}x{ny}x{nz}")
 
@@ -93,7 +114,7 @@ def _fill(m, n, rp, seed, lo=-1.0, hi=1.0):
     nnz = int(rp[-1])
     col = np.empty(nnz, np.int32)
     val = np.empty(nnz, np.float64)
-    _check(lib().bhsp_gen_random_fill(m, n, _p(rp), float(lo), float(hi), int(seed), _p(col),
+    _check(_lib().bhsp_gen_random_fill(m, n, _p(rp), float(lo), float(hi), int(seed), _p(col),
                                       _p(val)), "random_fill")
     return col, val
 
@@ -103,7 +124,7 @@ def powerlaw(m: int, n: int | None = None, alpha: float = POWERLAW_ALPHA,
              empty_frac: float = POWERLAW_EMPTY, seed: int = 2) -> CSR:
     n = m if n is None else n
     rp = np.empty(m + 1, np.int32)
-    _check(lib().bhsp_gen_powerlaw_rows(m, float(alpha), float(xmin), min(int(max_len), n),
+    _check(_lib().bhsp_gen_powerlaw_rows(m, float(alpha), float(xmin), min(int(max_len), n),
                                         float(empty_frac), int(seed), _p(rp)), "powerlaw_rows")
     col, val = _fill(m, n, rp, seed + 1000)
     return CSR(m, n, rp, col, val, f"powerlaw_{m}")
@@ -111,7 +132,7 @@ def powerlaw(m: int, n: int | None = None, alpha: float = POWERLAW_ALPHA,
 
 def density(m: int, n: int, dens: float, seed: int = 3) -> CSR:
     rp = np.empty(m + 1, np.int32)
-    _check(lib().bhsp_gen_density_rows(m, n, float(dens), int(seed), _p(rp)), "density_rows")
+    _check(_lib().bhsp_gen_density_rows(m, n, float(dens), int(seed), _p(rp)), "density_rows")
     col, val = _fill(m, n, rp, seed + 1000)
     return CSR(m, n, rp, col, val, f"density_{m}")
 
@@ -120,7 +141,7 @@ def mixed_rows(m: int, n: int, dense_row: int = -1, mean_len: float = 8.0,
                empty_frac: float = 0.0, seed: int = 4) -> CSR:
     """Poisson(mean_len) rows with an optional fully dense row and forced-empty rows."""
     rp = np.empty(m + 1, np.int32)
-    _check(lib().bhsp_gen_mixed_rows(m, n, int(dense_row), float(mean_len), float(empty_frac),
+    _check(_lib().bhsp_gen_mixed_rows(m, n, int(dense_row), float(mean_len), float(empty_frac),
                                      int(seed), _p(rp)), "mixed_rows")
     col, val = _fill(m, n, rp, seed + 1000)
     return CSR(m, n, rp, col, val, f"mixed_{m}")
@@ -129,11 +150,11 @@ def mixed_rows(m: int, n: int, dense_row: int = -1, mean_len: float = 8.0,
 def blockdiag(m: int, n: int | None = None, bs: int = 32, seed: int = 5) -> CSR:
     n = m if n is None else n
     rp = np.empty(m + 1, np.int32)
-    _check(lib().bhsp_gen_blockdiag_rows(m, n, int(bs), _p(rp)), "blockdiag_rows")
+    _check(_lib().bhsp_gen_blockdiag_rows(m, n, int(bs), _p(rp)), "blockdiag_rows")
     nnz = int(rp[-1])
     col = np.empty(nnz, np.int32)
     val = np.empty(nnz, np.float64)
-    _check(lib().bhsp_gen_blockdiag_fill(m, n, int(bs), -1.0, 1.0, int(seed), _p(rp), _p(col),
+    _check(_lib().bhsp_gen_blockdiag_fill(m, n, int(bs), -1.0, 1.0, int(seed), _p(rp), _p(col),
                                          _p(val)), "blockdiag_fill")
     return CSR(m, n, rp, col, val, f"blockdiag{bs}_{m}")
 

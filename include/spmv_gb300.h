@@ -96,10 +96,14 @@ int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tiles_per_worker, int* wa
 int bhsp_set_x(bhsp_spmv* h, const void* x);
 /* Streamed SpMVs over many right-hand sides held in host memory: y_host[i] = A x_host[i] for
  * i = 0..count-1, with the upload of x_{i+1} and the download of y_{i-1} overlapping the SpMV of
- * x_i (two device x / y buffers, separate upload, compute and download streams).  Blocks until
- * every y_host[i] is written.  F64 and F32 forms; host vectors in the handle's value type,
- * pinned (cudaHostAlloc / cudaHostRegister) for the copies to overlap.  No counterpart in the
- * reference, whose driver runs one SpMV per prepared x (spmv_cuda/main.cu:811-817). */
+ * x_i (two device x / y buffer pairs of its own, separate upload, compute and download streams).
+ * Blocks until every y_host[i] is written, or, on a failure, until none of its copies and
+ * kernels is still running.  The handle's own x and y (prepare_mem / set_x / run_benchmark)
+ * are not touched: a later run_benchmark computes with the x it held before.  The extra buffers
+ * (2 x (n + m) vector entries) are allocated on the first call and kept until free_mem.  F64
+ * and F32 forms; host vectors in the handle's value type, pinned (cudaHostAlloc /
+ * cudaHostRegister) for the copies to overlap.  No counterpart in the reference, whose driver
+ * runs one SpMV per prepared x (spmv_cuda/main.cu:811-817). */
 int bhsp_run_stream(bhsp_spmv* h, int count, const void* const* x_host, void* const* y_host);
 /* Enqueue y = A.x on `stream` (a cudaStream_t, NULL = the legacy default stream) and
  * return at once; bhsp_check() synchronises and reports a kernel-side failure. */
@@ -263,7 +267,13 @@ void bhsp_mlp_destroy(bhsp_mlp* m);
  * (tile partition, carry records, error word) lives in the fixed array above, so the call
  * performs no cudaMalloc, cudaFree or other allocating routine.
  *   - The first call on each device looks up the array's device address (with that device
- *     current) and caches it; make that first call before any stream capture.
+ *     current) and caches it for the rest of the process; make that first call before any
+ *     stream capture.  The cached address does not survive a reset of the device's primary
+ *     context (cudaDeviceReset): do not call this entry point across one.
+ *   - It always runs the tile kernel's per-slot chunk form with x gathered through L1 at a
+ *     fixed schedule (16 non-zeros per lane, 8 tiles per worker, 4 warps): the plan-time
+ *     choices of the other entry points (one-head form, L2-only gathers, learned or tuned
+ *     schedule) need counts read back from the device, which this call skips.
  *   - Every call shares the one array: calls whose work overlaps on the GPU (two streams, two
  *     host threads) race and must not be issued; calls in sequence are safe.
  *   - The call enqueues on `stream` and synchronises it before returning; it returns

@@ -6,9 +6,15 @@ Test infrastructure only.  Each wrapper names the reference code it restates
 * :func:`partition`         spmv_cuda/utils_cuda.h:6-31, spmv_cuda/kernels_cuda.h:39-53, 114-145
 * :func:`bitflags`          spmv_cuda/kernels_cuda.h:114-148
 * :func:`bhsparse`          spmv_cuda/kernels_cuda.h:7-269 + spmv_cuda/bhsparse_spmv_cuda.h:166-222
+* :func:`bhsparse_kernel`   spmv_cuda/kernels_cuda.h:7-269 alone; :func:`calibrate` the host
+                            steps spmv_cuda/bhsparse_spmv_cuda.h:166-222
 * :func:`csr_serial`        spmv_cuda/main.cu:755-761
 * :func:`csr_omp`           spmv_cuda/main.cu:370-393
 * :func:`csr_dot2`          FP64 compensated oracle (Ogita-Rump-Oishi Dot2)
+
+and, where ``make -C oracle ref`` built oracle/_ref/libref.so, the reference's own host code
+compiled from its sources (:func:`ref_calibrate`, :func:`ref_serial`, :func:`ref_omp`), which
+pins the restatements above.
 """
 from __future__ import annotations
 
@@ -65,6 +71,17 @@ def lib() -> ctypes.CDLL:
                 f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _i32p, vp, vp,
                               ctypes.c_int, ctypes.c_int, vp, _i32p, vp, _i32p, _i32p, _i32p]
                 f.restype = ctypes.c_int
+            for name, vp in (("oracle_bhsparse_kernel_f64", _f64p),
+                             ("oracle_bhsparse_kernel_f32", _f32p)):
+                f = getattr(L, name)
+                f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _i32p, _i32p, vp, vp,
+                              ctypes.c_int, ctypes.c_int, vp, _i32p, vp, _i32p, _i32p]
+                f.restype = ctypes.c_int
+            for name, vp in (("oracle_calibrate_f64", _f64p), ("oracle_calibrate_f32", _f32p)):
+                f = getattr(L, name)
+                f.argtypes = [ctypes.c_int, _i32p, ctypes.c_int, _i32p, vp, ctypes.c_int, _i32p,
+                              vp, _i32p]
+                f.restype = None
             L.oracle_csr_serial_f64.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
             L.oracle_csr_serial_f32.argtypes = [ctypes.c_int, _i32p, _i32p, _f32p, _f32p, _f32p]
             L.oracle_csr_serial_rows_f64.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p,
@@ -173,6 +190,152 @@ def bhsparse(row_ptr, col, val, x, n: int | None = None, seg_h: int | None = Non
         raise ValueError("unsupported geometry")
     return BhsparseResult(y[:m], sidx[:nw], sval[:nw], spec[:2 * nd.value].reshape(-1, 2),
                           nd.value, bool(fl.value & 1))
+
+
+class KernelStage:
+    """What the simulated SpMV_kernel leaves before run_benchmark's host steps: the compacted
+    y, the synchronizer (one entry per warp) and the speculator (dirty tiles)."""
+
+    def __init__(self, y, sync_idx, sync_val, spec, ndirty):
+        self.y = y
+        self.sync_idx = sync_idx
+        self.sync_val = sync_val
+        self.speculator = spec
+        self.ndirty = ndirty
+
+
+def bhsparse_kernel(row_ptr, col, val, x, seg_h: int | None = None, step: int = STEP,
+                    y0=None) -> KernelStage:
+    """Lane-level simulation of SpMV_kernel alone (spmv_cuda/kernels_cuda.h:7-269)."""
+    rp = _c(row_ptr, np.int32)
+    ci = _c(col, np.int32)
+    m = rp.size - 1
+    nnz = int(rp[-1]) if m >= 0 else 0
+    if np.asarray(val).dtype == np.float32:
+        vt, vp, fn = np.float32, _f32p, lib().oracle_bhsparse_kernel_f32
+        seg_h = SEG_H_F32 if seg_h is None else seg_h
+    else:
+        vt, vp, fn = np.float64, _f64p, lib().oracle_bhsparse_kernel_f64
+        seg_h = SEG_H_F64 if seg_h is None else seg_h
+    v, xx = _c(val, vt), _c(x, vt)
+    y = np.zeros(max(m, 1), dtype=vt) if y0 is None else _c(y0, vt).copy()
+    nw = num_warps(nnz, seg_h, step)
+    sidx = np.zeros(max(nw, 1), dtype=np.int32)
+    sval = np.zeros(max(nw, 1), dtype=vt)
+    spec = np.zeros(2 * max(num_tiles(nnz, LANES * seg_h), 1), dtype=np.int32)
+    nd = ctypes.c_int(0)
+    rc = fn(m, xx.size, nnz, _p(rp, _i32p), _p(ci, _i32p), _p(v, vp), _p(xx, vp), int(seg_h),
+            int(step), _p(y, vp), _p(sidx, _i32p), _p(sval, vp), _p(spec, _i32p),
+            ctypes.byref(nd))
+    if rc < 0:
+        raise ValueError("unsupported geometry")
+    return KernelStage(y[:m].copy(), sidx[:nw].copy(), sval[:nw].copy(),
+                       spec[:2 * nd.value].copy(), nd.value)
+
+
+def calibrate(row_ptr, stage: KernelStage):
+    """The oracle's restatement of run_benchmark's host steps (bhsparse_spmv_cuda.h:166-222)
+    applied to a copy of stage.y: (y, True if the fix-up would have read row_ptr[m+1])."""
+    rp = _c(row_ptr, np.int32)
+    m = rp.size - 1
+    vt = stage.y.dtype
+    vp = _f32p if vt == np.float32 else _f64p
+    fn = lib().oracle_calibrate_f32 if vt == np.float32 else lib().oracle_calibrate_f64
+    y = np.zeros(max(m, 1), vt)
+    y[:m] = stage.y
+    sidx, sval = _c(stage.sync_idx, np.int32), _c(stage.sync_val, vt)
+    spec = _c(stage.speculator, np.int32) if stage.ndirty else np.zeros(2, np.int32)
+    fl = ctypes.c_int(0)
+    fn(m, _p(rp, _i32p), int(sidx.size), _p(sidx, _i32p), _p(sval, vp), int(stage.ndirty),
+       _p(spec, _i32p), _p(y, vp), ctypes.byref(fl))
+    return y[:m], bool(fl.value & 1)
+
+
+# -- the reference's own host loops, compiled from its sources (oracle/_ref/libref.so) --------
+_REF_SO = os.path.join(_HERE, "_ref", "libref.so")
+_ref = None
+
+
+def ref_lib():
+    """oracle/_ref/libref.so (oracle/ref_harness.cpp around the reference's host calibration,
+    serial and OpenMP loops, built by ``make -C oracle ref``), or None where it was not built."""
+    global _ref
+    with _lock:
+        if _ref is None and os.path.exists(_REF_SO):
+            L = ctypes.CDLL(_REF_SO)
+            for sfx, vp in (("f64", _f64p), ("f32", _f32p)):
+                f = getattr(L, "ref_calibrate_" + sfx)
+                f.argtypes = [ctypes.c_int, _i32p, vp, vp, ctypes.c_int, vp, _i32p, _i32p,
+                              ctypes.c_int]
+                f.restype = None
+                f = getattr(L, "ref_serial_" + sfx)
+                f.argtypes = [ctypes.c_int, _i32p, _i32p, vp, vp, vp]
+                f.restype = None
+                f = getattr(L, "ref_omp_" + sfx)
+                f.argtypes = [ctypes.c_int, _i32p, _i32p, vp, vp, vp, ctypes.c_int, ctypes.c_int]
+                f.restype = None
+            _ref = L
+        return _ref
+
+
+def ref_calibrate(row_ptr, stage: KernelStage):
+    """The reference's own host calibration (spmv_cuda/bhsparse_spmv_cuda.h:170-222, compiled
+    from its source) applied to a copy of stage.y: (y[:m], value it wrote at y[m]).  row_ptr, y
+    and y_temp get one extra entry (row_ptr[m+1] = row_ptr[m]) so that the fix-up's read of
+    row_ptr[m+1] and write of y[m] for a dirty last tile stay inside the buffers."""
+    L = ref_lib()
+    rp = _c(row_ptr, np.int32)
+    m = rp.size - 1
+    rpp = np.concatenate([rp, rp[-1:]])
+    vt = stage.y.dtype
+    vp = _f32p if vt == np.float32 else _f64p
+    fn = L.ref_calibrate_f32 if vt == np.float32 else L.ref_calibrate_f64
+    y = np.zeros(m + 1, vt)
+    y[:m] = stage.y
+    yt = np.zeros(m + 1, vt)
+    sidx, sval = _c(stage.sync_idx, np.int32), _c(stage.sync_val, vt)
+    spec = _c(stage.speculator, np.int32) if stage.ndirty else np.zeros(2, np.int32)
+    fn(int(sidx.size), _p(sidx, _i32p), _p(sval, vp), _p(y, vp), int(stage.ndirty), _p(yt, vp),
+       _p(spec, _i32p), _p(rpp, _i32p), m)
+    return y[:m], y[m]
+
+
+def ref_serial(row_ptr, col, val, x) -> np.ndarray:
+    """The reference's own serial CSR loop (spmv_cuda/main.cu:753-762, compiled from its source)."""
+    L = ref_lib()
+    rp, ci = _c(row_ptr, np.int32), _c(col, np.int32)
+    m = rp.size - 1
+    vt = np.float32 if np.asarray(val).dtype == np.float32 else np.float64
+    vp = _f32p if vt == np.float32 else _f64p
+    fn = L.ref_serial_f32 if vt == np.float32 else L.ref_serial_f64
+    v, xx = _c(val, vt), _c(x, vt)
+    y = np.zeros(max(m, 1), vt)
+    fn(m, _p(rp, _i32p), _p(ci, _i32p), _p(v, vp), _p(xx, vp), _p(y, vp))
+    return y[:m]
+
+
+def ref_omp(row_ptr, col, val, x, threads: int, runs: int = 1, y=None) -> np.ndarray:
+    """The reference's own OpenMP CSR loop (spmv_cuda/main.cu:377-393, compiled from its
+    source): `runs` passes on `threads` host threads, into ``y`` when given (float64, no copies
+    of the inputs when they are already contiguous int32 / float64)."""
+    L = ref_lib()
+    rp, ci = _c(row_ptr, np.int32), _c(col, np.int32)
+    m = rp.size - 1
+    v, xx = _c(val, np.float64), _c(x, np.float64)
+    if y is None:
+        y = np.zeros(max(m, 1), np.float64)
+    L.ref_omp_f64(m, _p(rp, _i32p), _p(ci, _i32p), _p(v, _f64p), _p(xx, _f64p), _p(y, _f64p),
+                  int(runs), int(threads))
+    return y[:m]
+
+
+def gen_library_path() -> str:
+    """oracle/_build/libgen.so: the package's seeded workload generators (csrc/gen.cpp) built on
+    their own by oracle/Makefile, for CPU code that must not load the GPU library."""
+    so = os.path.join(_HERE, "_build", "libgen.so")
+    if not os.path.exists(so):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return so
 
 
 def csr_serial(row_ptr, col, val, x) -> np.ndarray:

@@ -3,9 +3,9 @@
 known_6x6.json
     The reference's only known-answer case, the 6x6 matrix of
     spmv_cuda/main.cu:449-451 (row_ptr, col_idx, val = 1..15) with x = 1
-    (main.cu:472-474).  When the reference tree is mounted (REFERENCE_ROOT, default
-    /root/reference) the arrays are parsed from main.cu itself; otherwise the committed
-    copy is reused.  Expected y, tile_ptr and bit-flag words are computed here by a
+    (main.cu:472-474).  When the reference tree is given (first argument, or the
+    REFERENCE_ROOT environment variable) the arrays are parsed from its main.cu; otherwise
+    the committed copy is reused.  Expected y, tile_ptr and bit-flag words are computed here by a
     pure-Python restatement of the reference formulas (independent of oracle/oracle.c):
       * y: the serial loop, main.cu:480-486;
       * tile_ptr: binary_search_right_boundary_kernel (utils_cuda.h:6-31) at every tile
@@ -20,18 +20,19 @@ cases.npz
     partial sum exact, so y is compared bit for bit (the reference's own check,
     main.cu:789-806).
 
-Run:  python tests/golden/make_golden.py
+Run:  python tests/golden/make_golden.py [REFERENCE_TREE]
 """
 from __future__ import annotations
 
 import json
 import os
 import re
+import sys
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE_ROOT", "")
 GEOMS = (4, 8, 16, 32)
 
 

@@ -153,3 +153,64 @@ def test_error_metrics():
     assert oracle.componentwise_error(y, ys, s) == pytest.approx(5e-14, rel=1e-3)
     assert oracle.componentwise_error(np.array([0.0, 0, 1.0]), np.zeros(3), s) == float("inf")
     assert oracle.normwise_error(ys, y) == pytest.approx(1e-13 / np.sqrt(5), rel=1e-3)
+
+
+# -- pinned to the reference's own host code, compiled from its sources ---------------------
+# oracle/_ref/libref.so is built by `make -C oracle ref` from the reference tree (build() does
+# it where the tree is present); without it these tests skip.
+needs_ref = pytest.mark.skipif(oracle.ref_lib() is None,
+                               reason="oracle/_ref/libref.so not built (no reference tree)")
+
+
+def _random_real_csr(rng, dtype):
+    rp, col, _, _ = _random_int_csr(rng)
+    val = rng.uniform(-1.0, 1.0, int(rp[-1])).astype(dtype)
+    x = rng.uniform(-1.0, 1.0, int(col.max(initial=0)) + 1).astype(dtype)
+    return rp, col, val, x
+
+
+@needs_ref
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_calibration_matches_reference_code(dtype):
+    """The oracle's host calibration (inter-warp += and the speculative fix-up of dirty tiles)
+    gives bit for bit the y of the reference's own run_benchmark host code
+    (spmv_cuda/bhsparse_spmv_cuda.h:170-222) on the same kernel output, for 300 seeded real-
+    valued matrices with empty rows, dirty tiles and dirty last tiles.  Where the last tile is
+    dirty the reference reads row_ptr[m+1] and writes y[m]; with one padded entry that write
+    is 0 and rows 0..m-1 agree with the oracle's guarded loop."""
+    rng = np.random.default_rng(101)
+    dirty_cases = last_dirty = 0
+    for _ in range(300):
+        rp, col, val, x = _random_real_csr(rng, dtype)
+        st = oracle.bhsparse_kernel(rp, col, val, x)
+        y_o, oob = oracle.calibrate(rp, st)
+        y_r, y_m = oracle.ref_calibrate(rp, st)
+        assert np.array_equal(y_o, y_r)
+        assert y_m == 0
+        dirty_cases += st.ndirty > 0
+        last_dirty += oob
+    assert dirty_cases > 100 and last_dirty > 20
+
+
+@needs_ref
+def test_known_6x6_through_reference_calibration(known):
+    rp, ci = np.array(known["row_ptr"], np.int32), np.array(known["col_idx"], np.int32)
+    st = oracle.bhsparse_kernel(rp, ci, np.array(known["val"]), np.array(known["x"]))
+    y, _ = oracle.ref_calibrate(rp, st)
+    assert y.tolist() == [float(v) for v in known["y"]]
+
+
+@needs_ref
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_serial_and_openmp_loops_match_reference_code(dtype):
+    """The oracle's serial loop is bit-identical to the reference's own (spmv_cuda/main.cu:
+    753-762), and so is the reference's OpenMP loop (main.cu:377-393) at 1, 4 and all threads:
+    each row is summed in row order by one thread."""
+    rng = np.random.default_rng(102)
+    for _ in range(60):
+        rp, col, val, x = _random_real_csr(rng, dtype)
+        y_o = oracle.csr_serial(rp, col, val, x)
+        assert np.array_equal(y_o, oracle.ref_serial(rp, col, val, x))
+        if dtype == np.float64:
+            for t in (1, 4, os.cpu_count() or 1):
+                assert np.array_equal(y_o, oracle.ref_omp(rp, col, val, x, t, runs=2))

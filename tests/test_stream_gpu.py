@@ -70,3 +70,25 @@ def test_stream_rejects_mixed_and_nulls(cuda_ok):
                          np.zeros(a.m)) == 0
     assert h.run_stream([0], [y.data_ptr()]) == sp.BHSPARSE_INVALID_ARGUMENT
     h.close()
+
+
+def test_run_benchmark_after_stream_keeps_prepared_x(cuda_ok):
+    """run_stream works in buffers of its own: the x given to prepare_mem (or the last set_x)
+    is still the one run_benchmark uses afterwards, and y on the device is not overwritten."""
+    a = gen.powerlaw(30000, seed=5)
+    val = gen.uniform_int(a.nnz, 8, 10)
+    x0 = gen.uniform_int(a.n, 9, 10)
+    y_ref = oracle.csr_serial(a.row_ptr, a.col, val, x0)
+    h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    y = np.zeros(a.m)
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, val, x0, y) == 0
+    assert h.run_benchmark() == 0
+    xs = [_pinned(gen.uniform_int(a.n, 60 + i, 10)) for i in range(3)]
+    ys = [_pinned(np.zeros(a.m)) for _ in range(3)]
+    assert h.run_stream([v.data_ptr() for v in xs], [v.data_ptr() for v in ys]) == 0
+    assert h.get_y() == 0  # the y of the run_benchmark before the stream
+    assert np.array_equal(y, y_ref)
+    y[:] = -1.0
+    assert h.run_benchmark() == 0 and h.get_y() == 0
+    assert np.array_equal(y, y_ref)
+    h.close()

@@ -75,3 +75,24 @@ def test_noalloc_rejects_too_large_and_invalid(cuda_ok):
     yr = oracle.csr_serial(a.row_ptr, a.col, a.val, np.ones(a.n))
     scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, np.ones(a.n))
     assert oracle.componentwise_error(y.cpu().numpy(), yr, scale) <= TOL_F64
+
+
+@pytest.mark.parametrize("validate", [0, 1])
+def test_noalloc_allocates_no_device_memory(cuda_ok, validate):
+    """After a warm-up call (which loads the kernels' module), further calls leave the driver's
+    free device memory unchanged, with and without the CSR validation pass."""
+    import torch
+    a = gen.powerlaw(200_000, seed=23)
+    rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
+    val = torch.from_numpy(a.val).cuda()
+    x = torch.from_numpy(gen.uniform(a.n, 33)).cuda()
+    y = torch.zeros(a.m, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        assert _noalloc(rp, ci, val, x, y, a.m, a.n, a.nnz, validate) == sp.BHSPARSE_SUCCESS
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        assert _noalloc(rp, ci, val, x, y, a.m, a.n, a.nnz, validate) == sp.BHSPARSE_SUCCESS
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
