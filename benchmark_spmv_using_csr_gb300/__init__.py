@@ -8,7 +8,7 @@ CUDA kernels in ``csrc/``.
 from .api import (  # noqa: F401
     BHSPARSE_CUDA_ERROR, BHSPARSE_DEVICE_CHECK_FAILED, BHSPARSE_INVALID_ARGUMENT,
     BHSPARSE_INVALID_CSR, BHSPARSE_NOALLOC_TOO_LARGE, BHSPARSE_NOT_PREPARED, BHSPARSE_OUT_OF_MEMORY,
-    BHSPARSE_SUCCESS,
+    BHSPARSE_SUCCESS, SCHEDULE_CALLER, SCHEDULE_DEFAULT, SCHEDULE_LEARNED, SCHEDULE_SWEEP,
     BHSPARSE_UNSUPPORTED_VALUE_TYPE, DEFAULT_CONFIG, VALUE_F32, VALUE_F64, VALUE_MIXED_BF16,
     VALUE_MIXED_F32, VALUE_NAMES, BhsparseSpmvCuda, Plan, SpmvError, bitflags, host_dtype,
     partition, validate_csr, version)

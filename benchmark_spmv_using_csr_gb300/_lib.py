@@ -36,6 +36,8 @@ SIGNATURES = {
     "bhsp_last_error": (c_char_p, [c_void_p]),
     "bhsp_set_device": (c_int, [c_void_p, c_int]),
     "bhsp_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
+    "bhsp_set_tuner": (c_int, [c_void_p, c_char_p]),
+    "bhsp_get_schedule_source": (c_int, [c_void_p, P_int, ctypes.POINTER(ctypes.c_float)]),
     "bhsp_get_config": (c_int, [c_void_p, P_int, P_int, P_int, P_int]),
     "bhsp_set_x": (c_int, [c_void_p, c_void_p]),
     "bhsp_run_stream": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
@@ -87,6 +89,9 @@ SIGNATURES = {
     "bhsp_autotune": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                               c_void_p, c_int, c_int, c_void_p, P_int, c_void_p]),
     "bhsp_row_features": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p]),
+    "bhsp_choose_schedule": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                     c_void_p, c_void_p, c_char_p, P_int, P_int, P_int, P_int,
+                                     P_int, ctypes.POINTER(ctypes.c_float), c_void_p]),
     "bhsp_features_from_counts": (None, [c_int, c_int, c_void_p, c_void_p]),
     "bhsp_spmv_f64_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                                       c_int, c_int, c_int, c_void_p]),

@@ -32,6 +32,9 @@ BHSPARSE_DEVICE_CHECK_FAILED = -6
 BHSPARSE_OUT_OF_MEMORY = -7
 BHSPARSE_NOALLOC_TOO_LARGE = -8
 
+# where a schedule came from (bhsp_choose_schedule / bhsp_get_schedule_source)
+SCHEDULE_CALLER, SCHEDULE_DEFAULT, SCHEDULE_LEARNED, SCHEDULE_SWEEP = 0, 1, 2, 3
+
 VALUE_F64 = 0
 VALUE_F32 = 1
 VALUE_MIXED_F32 = 2
@@ -115,6 +118,16 @@ class BhsparseSpmvCuda:
 
     def set_device(self, device: int) -> int:
         return self._L.bhsp_set_device(self._h, int(device))
+
+    def set_tuner(self, path: str | None) -> int:
+        """Network file for prepare_mem's schedule choice (None = the library's, "" = none)."""
+        return self._L.bhsp_set_tuner(self._h, None if path is None else path.encode())
+
+    def schedule_source(self) -> tuple[int, float]:
+        """(BHSP_SCHEDULE_* source of the schedule in use, the network's confidence)."""
+        src, conf = ctypes.c_int(), ctypes.c_float()
+        self._L.bhsp_get_schedule_source(self._h, ctypes.byref(src), ctypes.byref(conf))
+        return src.value, float(conf.value)
 
     def set_config(self, seg: int = 0, tiles_per_worker: int = 0, warps_per_cta: int = 0,
                    stages: int = -1) -> int:

@@ -1,6 +1,7 @@
 // capi.cu -- the C ABI (include/spmv_gb300.h): handle API mirroring bhsparse_spmv_cuda
 // (spmv_cuda/bhsparse_spmv_cuda.h:7-351) and the device-pointer plan API.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -414,6 +415,11 @@ struct bhsp_spmv {
     bool platform = false;
     bool prepared = false;
     TileConfig cfg = make_config(0, 0, 0, -1, BHSP_VALUE_F64);  // reset for h->vt in bhsp_create
+    bool cfg_user = false;        // bhsp_set_config was called: prepare_mem keeps cfg
+    bool tuner_default = true;    // bhsp_set_tuner not called (or NULL): the library's network
+    std::string tuner_path;       // otherwise this network file ("" = none)
+    int sched_source = BHSP_SCHEDULE_DEFAULT;
+    float sched_conf = 0.f;
     int m = 0, n = 0, nnz = 0;
     int* d_row_ptr = nullptr;
     int* d_col = nullptr;
@@ -484,6 +490,22 @@ extern "C" int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int 
     TileConfig c = make_config(seg, tiles_per_worker, warps_per_cta, stages, h->vt);
     if (!config_ok(c, h->vt)) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "unsupported tile config");
     h->cfg = c;
+    h->cfg_user = true;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_set_tuner(bhsp_spmv* h, const char* path) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (h->prepared) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "set_tuner after prepare_mem");
+    h->tuner_default = path == nullptr;
+    h->tuner_path = path ? path : "";
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_get_schedule_source(const bhsp_spmv* h, int* source, float* confidence) {
+    if (!h) return BHSPARSE_INVALID_ARGUMENT;
+    if (source) *source = h->cfg_user ? BHSP_SCHEDULE_CALLER : h->sched_source;
+    if (confidence) *confidence = h->cfg_user ? 0.f : h->sched_conf;
     return BHSPARSE_SUCCESS;
 }
 
@@ -590,14 +612,44 @@ extern "C" int bhsp_prepare_mem(bhsp_spmv* h, int m, int n, int nnz, const int* 
     if (rc) return rc;
     rc = upload_values(h, h->d_x, x, (size_t)n, false);
     if (rc) return rc;
+    rc = validate_on_device(h->d_row_ptr, h->d_col, m, n, nnz, h->stream, &h->last_error);
+    if (rc) {
+        handle_release(h);
+        return rc;
+    }
+    if (!h->cfg_user) {
+        // the schedule: the learned network's pick, or the sweep below its confidence threshold
+        // (which runs SpMVs into d_y, so the caller's initial y is uploaded after it)
+        int c[4];
+        rc = bhsp_choose_schedule(h->vt, m, n, nnz, h->d_row_ptr, h->d_col, h->d_val, h->d_x,
+                                  h->d_y, h->tuner_default ? nullptr : h->tuner_path.c_str(),
+                                  &c[0], &c[1], &c[2], &c[3], &h->sched_source, &h->sched_conf,
+                                  h->stream);
+        if (rc) {
+            handle_release(h);
+            h->last_error = "schedule choice failed (tuner network file missing or malformed?)";
+            return rc;
+        }
+        h->cfg = make_config(c[0], c[1], c[2], c[3], h->vt);
+    }
+    if (const char* lg = std::getenv("BHSP_LOG_SCHEDULE"); lg && *lg && *lg != '0') {
+        static const char* const kSource[] = {"the caller (bhsp_set_config)", "the fixed default",
+                                              "the learned network", "the autotune sweep"};
+        const int src = h->cfg_user ? BHSP_SCHEDULE_CALLER : h->sched_source;
+        std::fprintf(stderr,
+                     "bhsp: m=%d nnz=%d schedule (%d, %d, %d, %d) from %s (confidence %.3f)\n", m,
+                     nnz, h->cfg.seg, h->cfg.tiles_per_worker, h->cfg.warps_per_cta, h->cfg.stages,
+                     kSource[src & 3], (double)(h->cfg_user ? 0.f : h->sched_conf));
+    }
     rc = upload_values(h, h->d_y, y, (size_t)m, false);
     if (rc) return rc;
     bhsp_plan* p = nullptr;
-    rc = bhsp_plan_create(&p, h->vt, m, n, nnz, h->d_row_ptr, h->d_col, h->cfg.seg,
-                          h->cfg.tiles_per_worker, h->cfg.warps_per_cta, h->cfg.stages, h->stream);
+    rc = spmv::plan_create_impl(&p, h->vt, m, n, nnz, h->d_row_ptr, h->d_col, h->cfg.seg,
+                                h->cfg.tiles_per_worker, h->cfg.warps_per_cta, h->cfg.stages,
+                                h->stream, false);
     if (rc) {
         handle_release(h);
-        h->last_error = rc == BHSPARSE_INVALID_CSR ? "invalid CSR (row_ptr or col_idx)" : "plan creation failed";
+        h->last_error = "plan creation failed";
         return rc;
     }
     h->plan = p;

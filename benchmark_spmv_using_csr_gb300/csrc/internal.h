@@ -66,6 +66,7 @@ struct PlainLaunch {
 };
 cudaError_t launch_plain_f64(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_plain_f32(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
+int plain_f32_smem_bytes(const TileConfig& cfg);
 
 // spmv_mixed.cu: mixed forms (FP32 / BF16 values, FP32 x and y, compensated FP32
 // accumulation, FP64 carries and records)
@@ -86,6 +87,8 @@ struct MixedLaunch {
     bool x_l2 = false;      // the plan's choice of L2-only x gathers
 };
 cudaError_t launch_mixed(const MixedLaunch& a, const TileConfig& cfg, cudaStream_t st);
+cudaError_t launch_mixed_bf16(const MixedLaunch& a, const TileConfig& cfg, cudaStream_t st);
+int mixed_bf16_smem_bytes(const TileConfig& cfg);
 cudaError_t launch_convert_from_f64(const double* src, void* dst, size_t n, bool to_bf16,
                                     cudaStream_t st);
 cudaError_t launch_convert_to_f64(const float* src, double* dst, size_t n, cudaStream_t st);

@@ -1,6 +1,9 @@
-// spmv_plain.cu -- plain FP64 / FP32 forms (the reference's USE_DOUBLE=1 / USE_DOUBLE=0
-// builds, spmv_cuda/common.h:27-31): values, x, y, accumulation and carries all in the
-// value type, one fused multiply-add per non-zero.
+// policies_plain.cuh -- arithmetic policies of the plain forms (the reference's USE_DOUBLE=1 /
+// USE_DOUBLE=0 builds, spmv_cuda/common.h:27-31): values, x, y, accumulation and carries all in
+// the value type, one fused multiply-add per non-zero.  Shared by spmv_plain_f64.cu and
+// spmv_plain_f32.cu, one translation unit per value type so that the build runs them in
+// parallel.
+#pragma once
 #include "internal.h"
 #include "tile_kernel_tma.cuh"
 
@@ -53,7 +56,7 @@ struct PolF32 {
 };
 
 template <class P>
-static cudaError_t launch_plain_any(const PlainLaunch& l, const TileConfig& cfg, cudaStream_t st) {
+inline cudaError_t launch_plain_any(const PlainLaunch& l, const TileConfig& cfg, cudaStream_t st) {
     TileArgs<P> a;
     a.row_ptr = l.row_ptr;
     a.col = l.col;
@@ -71,17 +74,6 @@ static cudaError_t launch_plain_any(const PlainLaunch& l, const TileConfig& cfg,
     a.one_head = l.one_head;
     a.x_l2 = l.x_l2;
     return launch_tiles_any<P>(a, cfg, st);
-}
-
-cudaError_t launch_plain_f64(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st) {
-    return launch_plain_any<PolF64>(a, cfg, st);
-}
-cudaError_t launch_plain_f32(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st) {
-    return launch_plain_any<PolF32>(a, cfg, st);
-}
-
-int plain_smem_bytes(bool f64, const TileConfig& cfg) {
-    return f64 ? tma_smem_bytes<PolF64>(cfg) : tma_smem_bytes<PolF32>(cfg);
 }
 
 }  // namespace spmv

@@ -113,14 +113,16 @@ __device__ __forceinline__ void swz_cols8(const unsigned char* base, uint32_t of
     }
 }
 
-template <typename XT>
+// x entries of one 8-slot chunk: through L1, or from L2 only (XL2, the plan's choice for
+// columns without locality)
+template <bool XL2, typename XT>
 __device__ __forceinline__ void gather8(const XT* __restrict__ x, const int (&c)[8], uint64_t pol,
                                         XT (&xv)[8]) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) xv[i] = c[i] >= 0 ? ld_x(x + c[i], pol) : XT(0);
+    for (int i = 0; i < 8; ++i) xv[i] = c[i] >= 0 ? ld_x_sel<XL2>(x + c[i], pol) : XT(0);
 }
 
-template <class P, int S, int WARPS, int NSTAGE, bool OH>
+template <class P, int S, int WARPS, int NSTAGE, bool OH, bool XL2>
 __global__ void __launch_bounds__(WARPS * 32, 1)
     k_tiles_tma(TileArgs<P> a, const __grid_constant__ StreamMaps maps, int tpw, int nworkers,
                 int ntiles) {
@@ -198,7 +200,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     auto gather_chunk = [&](int t, int c, XT (&xv)[8]) {
         int cc[8];
         swz_cols8(vslot(t) + L::VREG, lane * CRUN + c * 32, cc);
-        gather8(a.x, cc, pol_x, xv);
+        gather8<XL2>(a.x, cc, pol_x, xv);
     };
 
 #pragma unroll
@@ -348,7 +350,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     if (!rec_written && lane == 0) a.rec_row[worker] = -1;
 }
 
-template <class P, int S, int WARPS, int NSTAGE, bool OH>
+template <class P, int S, int WARPS, int NSTAGE, bool OH, bool XL2>
 cudaError_t launch_tma_kernel(const TileArgs<P>& a, const StreamMaps& maps, int tpw, int nworkers,
                               int ntiles, int bytes, cudaStream_t st) {
     // the shared-memory opt-in is a per-device function attribute: set it once per device
@@ -359,14 +361,14 @@ cudaError_t launch_tma_kernel(const TileArgs<P>& a, const StreamMaps& maps, int 
     if (e != cudaSuccess) return e;
     const unsigned long long bit = 1ull << (dev & 63);
     if (!(attr_set.load(std::memory_order_acquire) & bit)) {
-        e = cudaFuncSetAttribute(k_tiles_tma<P, S, WARPS, NSTAGE, OH>,
+        e = cudaFuncSetAttribute(k_tiles_tma<P, S, WARPS, NSTAGE, OH, XL2>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit, std::memory_order_release);
     }
     const int blocks = (nworkers + WARPS - 1) / WARPS;
-    k_tiles_tma<P, S, WARPS, NSTAGE, OH><<<blocks, WARPS * 32, bytes, st>>>(a, maps, tpw, nworkers,
-                                                                           ntiles);
+    k_tiles_tma<P, S, WARPS, NSTAGE, OH, XL2><<<blocks, WARPS * 32, bytes, st>>>(a, maps, tpw,
+                                                                                nworkers, ntiles);
     return cudaSuccess;
 }
 
@@ -388,14 +390,24 @@ cudaError_t launch_tiles_tma_t(const TileArgs<P>& a, int tpw, int nworkers, int 
             return launch_tiles<P>(a, c, st);
         }
         cudaError_t e;
-        if constexpr (sizeof(typename P::Acc) <= 8)  // scalar accumulators: either form
-            e = a.one_head ? launch_tma_kernel<P, S, WARPS, NSTAGE, true>(a, maps, tpw, nworkers,
-                                                                         ntiles, bytes, st)
-                           : launch_tma_kernel<P, S, WARPS, NSTAGE, false>(a, maps, tpw, nworkers,
-                                                                          ntiles, bytes, st);
-        else
-            e = launch_tma_kernel<P, S, WARPS, NSTAGE, false>(a, maps, tpw, nworkers, ntiles,
-                                                              bytes, st);
+        if constexpr (sizeof(typename P::Acc) <= 8) {  // scalar accumulators: either form
+            // chunk form and x gather path, both fixed by the plan
+            if (a.one_head && a.x_l2)
+                e = launch_tma_kernel<P, S, WARPS, NSTAGE, true, true>(a, maps, tpw, nworkers,
+                                                                       ntiles, bytes, st);
+            else if (a.one_head)
+                e = launch_tma_kernel<P, S, WARPS, NSTAGE, true, false>(a, maps, tpw, nworkers,
+                                                                        ntiles, bytes, st);
+            else if (a.x_l2)
+                e = launch_tma_kernel<P, S, WARPS, NSTAGE, false, true>(a, maps, tpw, nworkers,
+                                                                        ntiles, bytes, st);
+            else
+                e = launch_tma_kernel<P, S, WARPS, NSTAGE, false, false>(a, maps, tpw, nworkers,
+                                                                         ntiles, bytes, st);
+        } else {
+            e = launch_tma_kernel<P, S, WARPS, NSTAGE, false, false>(a, maps, tpw, nworkers,
+                                                                     ntiles, bytes, st);
+        }
         if (e != cudaSuccess) return e;
     }
     if (a.phase & 2) {

@@ -1,7 +1,7 @@
 // tuner.cu -- schedule autotuner and the row-length features the learned tuner reads.
 //
 // The autotuner times every candidate schedule (non-zeros per lane S, tiles per worker,
-// warps per CTA) of the tile kernel on the caller's matrix and reports the per-candidate time
+// warps per CTA, direct or TMA-staged stream) of the tile kernel on the caller's matrix and reports the per-candidate time
 // and the fastest.  It only picks a schedule; every candidate computes the same y (the
 // arithmetic does not depend on the schedule beyond summation order).  No counterpart in the
 // reference, whose tile geometry is fixed at compile time (spmv_cuda/common.h:39-48).
@@ -16,13 +16,17 @@
 namespace {
 
 struct Cand {
-    int seg, tpw, warps;
+    int seg, tpw, warps, stages;
 };
-// S in {8,16,32} x tiles-per-worker in {1,4,8,16} x warps-per-CTA in {4,8}; direct loads.
+// Direct loads: S in {8,16,32} x tiles-per-worker in {1,4,8,16} x warps-per-CTA in {4,8}; then
+// the TMA-staged ring (2 or 3 tiles) at S in {8,16} x tiles-per-worker in {4,8}, 4 warps.
 const Cand kCands[] = {
-    {8, 1, 4},  {8, 1, 8},  {8, 4, 4},  {8, 4, 8},  {8, 8, 4},  {8, 8, 8},  {8, 16, 4},  {8, 16, 8},
-    {16, 1, 4}, {16, 1, 8}, {16, 4, 4}, {16, 4, 8}, {16, 8, 4}, {16, 8, 8}, {16, 16, 4}, {16, 16, 8},
-    {32, 1, 4}, {32, 1, 8}, {32, 4, 4}, {32, 4, 8}, {32, 8, 4}, {32, 8, 8}, {32, 16, 4}, {32, 16, 8},
+    {8, 1, 4, 0},  {8, 1, 8, 0},  {8, 4, 4, 0},  {8, 4, 8, 0},  {8, 8, 4, 0},  {8, 8, 8, 0},
+    {8, 16, 4, 0}, {8, 16, 8, 0}, {16, 1, 4, 0}, {16, 1, 8, 0}, {16, 4, 4, 0}, {16, 4, 8, 0},
+    {16, 8, 4, 0}, {16, 8, 8, 0}, {16, 16, 4, 0}, {16, 16, 8, 0}, {32, 1, 4, 0}, {32, 1, 8, 0},
+    {32, 4, 4, 0}, {32, 4, 8, 0}, {32, 8, 4, 0}, {32, 8, 8, 0}, {32, 16, 4, 0}, {32, 16, 8, 0},
+    {8, 4, 4, 2},  {8, 8, 4, 2},  {8, 4, 4, 3},  {8, 8, 4, 3},  {16, 4, 4, 2}, {16, 8, 4, 2},
+    {16, 4, 4, 3}, {16, 8, 4, 3},
 };
 constexpr int kNumCands = sizeof(kCands) / sizeof(kCands[0]);
 
@@ -36,7 +40,7 @@ extern "C" int bhsp_tune_candidate(int index, int* seg, int* tiles_per_worker, i
     if (seg) *seg = kCands[index].seg;
     if (tiles_per_worker) *tiles_per_worker = kCands[index].tpw;
     if (warps_per_cta) *warps_per_cta = kCands[index].warps;
-    if (stages) *stages = 0;
+    if (stages) *stages = kCands[index].stages;
     return BHSPARSE_SUCCESS;
 }
 
@@ -71,9 +75,15 @@ extern "C" int bhsp_autotune(int value_type, int m, int n, int nnz, const int* d
     float best_ms = 0.f;
     std::vector<float> t((size_t)reps);
     for (int i = 0; i < kNumCands && rc == BHSPARSE_SUCCESS; ++i) {
+        const spmv::TileConfig c{kCands[i].seg, kCands[i].tpw, kCands[i].warps, kCands[i].stages};
+        const int smem = spmv::tile_config_smem_bytes(value_type, c);
+        if (smem < 0 || smem > 227 * 1024) {  // a staged ring this value type cannot hold
+            ms_out[i] = INFINITY;
+            continue;
+        }
         bhsp_plan* p = nullptr;
-        rc = spmv::plan_create_impl(&p, value_type, m, n, nnz, d_row_ptr, d_col_idx, kCands[i].seg,
-                                    kCands[i].tpw, kCands[i].warps, 0, stream, false);
+        rc = spmv::plan_create_impl(&p, value_type, m, n, nnz, d_row_ptr, d_col_idx, c.seg,
+                                    c.tiles_per_worker, c.warps_per_cta, c.stages, stream, false);
         if (rc) break;
         for (int w = 0; w < warmup && rc == 0; ++w) rc = bhsp_plan_execute(p, d_val, d_x, d_y, stream);
         for (int r = 0; r < reps && rc == 0; ++r) {

@@ -175,21 +175,20 @@ class LearnedTuner:
         p = self.net.forward(np.atleast_2d(feats))
         return p.argmax(1), p.max(1)
 
-    def calibrate_threshold(self, feats, ms, target: float = 0.95, max_fallback: float = 0.2) -> float:
-        """Smallest confidence threshold whose non-fallback picks reach `target` of the best
-        time on average (searched on held-in data), capped so at most `max_fallback` of the
-        matrices fall back."""
+    def calibrate_threshold(self, feats, ms, floor: float = 0.95, max_fallback: float = 0.25) -> float:
+        """Confidence threshold from matrices the network was not fitted on: the smallest one
+        below which every pick slower than `floor` of the best time falls back to the sweep,
+        or, if that would send more than `max_fallback` of the matrices to the sweep, the
+        largest threshold within that budget."""
         pick, conf = self.predict(feats)
         frac = ms.min(1) / ms[np.arange(len(pick)), pick]
-        order = np.sort(np.unique(conf))
         self.threshold = 0.0
-        for th in np.concatenate([[0.0], order]):
+        for th in np.concatenate([[0.0], np.sort(np.unique(conf)) + 1e-7]):
             keep = conf >= th
             if (~keep).mean() > max_fallback:
                 break
-            mixed = np.where(keep, frac, 1.0)
             self.threshold = float(th)
-            if mixed.mean() >= target:
+            if not np.any(keep & (frac < floor)):
                 break
         return self.threshold
 
@@ -203,6 +202,9 @@ class LearnedTuner:
         return {"mean_frac_of_best": float(frac_with_fb.mean()),
                 "min_frac_of_best": float(frac_with_fb.min()),
                 "mean_frac_without_fallback": float(frac.mean()),
+                "min_frac_without_fallback": float(frac.min()),
+                "picks_below_95pct_kept": int(np.sum((frac < 0.95) & ~fb)),
+                "picks_below_95pct_without_fallback": int(np.sum(frac < 0.95)),
                 "fallback_rate": float(fb.mean()), "threshold": self.threshold}
 
     def choose(self, value_type: int, row_ptr, col_idx, val, x, y, n: int | None = None) -> dict:
@@ -219,17 +221,65 @@ class LearnedTuner:
         return {"index": best, "confidence": float(conf[0]), "fallback": True,
                 "config": tune.candidates()[best], "ms": ms}
 
-    def save(self, path: str) -> None:
-        np.savez(path, params=self.net.get_params(), mean=self.net.mean, std=self.net.std,
-                 threshold=np.float32(self.threshold), n_out=self.n_out, hidden=self.net.hidden,
-                 candidates=np.array(self.candidates if self.candidates else [], np.int32))
+    def save(self, path: str, value_type: int) -> None:
+        """Write the network file the C library reads (csrc/learned.cu): magic, value type,
+        sizes, threshold, input standardisation, candidate schedules, parameters."""
+        if self.candidates is None:
+            raise ValueError("only a network tied to candidate schedules can be saved")
+        write_network(path, value_type, self.net.hidden, self.threshold, self.net.mean,
+                      self.net.std, np.array(self.candidates, np.int32), self.net.get_params())
 
     @classmethod
     def load(cls, path: str) -> "LearnedTuner":
-        d = np.load(path)
-        cands = d["candidates"] if "candidates" in d.files and d["candidates"].size else None
-        t = cls(n_out=int(d["n_out"]), hidden=int(d["hidden"]), candidates=cands)
+        d = read_network(path)
+        t = cls(n_out=d["n_out"], hidden=d["hidden"], candidates=d["candidates"])
         t.net.set_params(d["params"])
         t.net.set_normalization(d["mean"], d["std"])
-        t.threshold = float(d["threshold"])
+        t.threshold = d["threshold"]
+        t.value_type = d["value_type"]
         return t
+
+
+MAGIC = b"BHSPTUN1"
+
+
+def write_network(path: str, value_type: int, hidden: int, threshold: float, mean, std,
+                  candidates: np.ndarray, params: np.ndarray) -> None:
+    """The little-endian network file of csrc/learned.cu."""
+    cands = np.ascontiguousarray(candidates, "<i4").reshape(-1, 4)
+    mean = np.ascontiguousarray(mean, "<f4")
+    std = np.ascontiguousarray(std, "<f4")
+    params = np.ascontiguousarray(params, "<f4")
+    with open(path, "wb") as f:
+        f.write(MAGIC)
+        f.write(np.array([value_type, mean.size, hidden, cands.shape[0]], "<i4").tobytes())
+        f.write(np.array([threshold], "<f4").tobytes())
+        f.write(mean.tobytes())
+        f.write(std.tobytes())
+        f.write(cands.tobytes())
+        f.write(np.array([params.size], "<i4").tobytes())
+        f.write(params.tobytes())
+
+
+def read_network(path: str) -> dict:
+    raw = open(path, "rb").read()
+    if raw[:8] != MAGIC:
+        raise ValueError(f"{path}: not a network file")
+    vt, n_in, hidden, n_out = (int(v) for v in np.frombuffer(raw, "<i4", 4, 8))
+    o = 24
+    threshold = float(np.frombuffer(raw, "<f4", 1, o)[0])
+    o += 4
+    mean = np.frombuffer(raw, "<f4", n_in, o).copy()
+    o += 4 * n_in
+    std = np.frombuffer(raw, "<f4", n_in, o).copy()
+    o += 4 * n_in
+    cands = np.frombuffer(raw, "<i4", 4 * n_out, o).reshape(n_out, 4).copy()
+    o += 16 * n_out
+    npar = int(np.frombuffer(raw, "<i4", 1, o)[0])
+    o += 4
+    params = np.frombuffer(raw, "<f4", npar, o).copy()
+    if o + 4 * npar != len(raw):
+        raise ValueError(f"{path}: trailing or missing bytes")
+    return {"value_type": vt, "n_in": n_in, "hidden": hidden, "n_out": n_out,
+            "threshold": threshold, "mean": mean, "std": std, "candidates": cands,
+            "params": params}

@@ -1,6 +1,9 @@
-"""Build the learned tuner's dataset on a GB300: seeded synthetic matrices, their 16 row-length
+"""Build the learned tuner's datasets on a GB300: seeded synthetic matrices, their 16 row-length
 features (computed on the device) and the autotuner's timing table for every candidate
-schedule (plain FP32 form, median of 3 CUDA-event-timed runs after 1 warm-up).
+schedule (median of 3 CUDA-event-timed runs after 1 warm-up, each after an L2-flushing write),
+for each value type: plain FP64, plain FP32, mixed FP32 and mixed BF16 storage.  Each matrix
+is generated once and timed in every value type; one timing file per value type
+(gb300_<f64|f32|mixed_f32|mixed_bf16>_timings.npz).
 
 Matrices: row counts log-uniform in [10,000, 8,000,000]; generator drawn from the batched
 workload's mix (2D / 3D stencil, power-law rows, uniform density, block-diagonal 32x32) plus a
@@ -9,7 +12,7 @@ stays under the non-zero budget); any matrix whose generator would exceed the bu
 (NNZ_CAP) is drawn with proportionally fewer rows.  Indices [0, 2000) train, [2000, 2200) are
 held out.
 
-    python -m benchmark_spmv_using_csr_gb300.tuner_data.build_dataset [out.npz] [count]
+    python -m benchmark_spmv_using_csr_gb300.tuner_data.build_dataset [out_dir] [count]
 """
 from __future__ import annotations
 
@@ -44,40 +47,64 @@ def draw(i: int):
     return kind, gen.batch_member(m, kind, seed)
 
 
-def main(out: str, count: int = 2200) -> None:
+def _load(path: str, count: int, k: int):
+    feats = np.zeros((count, 16), np.float32)
+    ms = np.zeros((count, k), np.float32)
+    meta = np.zeros((count, 3), np.int64)  # m, nnz, kind index
+    done = 0
+    if os.path.exists(path):  # resume
+        d = np.load(path)
+        if d["ms"].shape[1] == k:
+            done = min(int(d["done"]), count)
+            feats[:done], ms[:done], meta[:done] = (d["features"][:done], d["ms"][:done],
+                                                    d["meta"][:done])
+    return feats, ms, meta, done
+
+
+def main(out_dir: str, count: int = 2200, value_types=None) -> None:
     import torch
 
     import benchmark_spmv_using_csr_gb300 as sp
     from benchmark_spmv_using_csr_gb300 import tune
-    k = len(tune.candidates())
-    feats = np.zeros((count, tune.NUM_FEATURES), np.float32)
-    ms = np.zeros((count, k), np.float32)
-    meta = np.zeros((count, 3), np.int64)  # m, nnz, kind index
-    start = 0
-    if os.path.exists(out):  # resume
-        d = np.load(out)
-        done = int(d["done"])
-        feats[:done], ms[:done], meta[:done] = d["features"][:done], d["ms"][:done], d["meta"][:done]
-        start = done
+    vts = list(sp.VALUE_NAMES) if value_types is None else list(value_types)
+    cands = np.array(tune.candidates())
+    k = len(cands)
+    paths = {vt: os.path.join(out_dir, f"gb300_{sp.VALUE_NAMES[vt]}_timings.npz") for vt in vts}
+    state = {vt: _load(paths[vt], count, k) for vt in vts}
+    start = min(state[vt][3] for vt in vts)
     t0 = time.time()
     for i in range(start, count):
         kind, a = draw(i)
         rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
-        val = torch.from_numpy(a.val.astype(np.float32)).cuda()
-        x = torch.from_numpy(np.ones(a.n, np.float32)).cuda()
-        y = torch.zeros(a.m, dtype=torch.float32, device="cuda")
-        feats[i] = tune.row_features(rp, a.n)
-        ms[i], _ = tune.autotune(sp.VALUE_F32, rp, ci, val, x, y, warmup=1, reps=3)
-        meta[i] = (a.m, a.nnz, KINDS.index(kind))
-        del rp, ci, val, x, y
+        v64 = torch.from_numpy(a.val).cuda()
+        f = tune.row_features(rp, a.n)
+        for vt in vts:
+            feats, ms, meta, done = state[vt]
+            if i < done:
+                continue
+            if vt == sp.VALUE_F64:
+                val, xt = v64, torch.float64
+            elif vt == sp.VALUE_MIXED_BF16:
+                val, xt = v64.to(torch.bfloat16), torch.float32
+            else:
+                val, xt = v64.float(), torch.float32
+            x = torch.ones(a.n, dtype=xt, device="cuda")
+            y = torch.zeros(a.m, dtype=xt, device="cuda")
+            feats[i] = f
+            ms[i], _ = tune.autotune(vt, rp, ci, val, x, y, warmup=1, reps=3)
+            meta[i] = (a.m, a.nnz, KINDS.index(kind))
+            del val, x, y
+        del rp, ci, v64
         if (i + 1) % 100 == 0 or i + 1 == count:
-            np.savez(out, features=feats, ms=ms, meta=meta, done=i + 1, kinds=np.array(KINDS),
-                     candidates=np.array(tune.candidates()), nnz_cap=NNZ_CAP)
+            for vt in vts:
+                feats, ms, meta, _ = state[vt]
+                np.savez(paths[vt], features=feats, ms=ms, meta=meta, done=i + 1,
+                         kinds=np.array(KINDS), candidates=cands, nnz_cap=NNZ_CAP, value_type=vt)
             print(f"{i + 1}/{count} matrices, {time.time() - t0:.0f} s", flush=True)
             torch.cuda.empty_cache()
 
 
 if __name__ == "__main__":
     here = os.path.dirname(os.path.abspath(__file__))
-    out = sys.argv[1] if len(sys.argv) > 1 else os.path.join(here, "gb300_fp32_timings.npz")
+    out = sys.argv[1] if len(sys.argv) > 1 else here
     main(out, int(sys.argv[2]) if len(sys.argv) > 2 else 2200)

@@ -1,9 +1,18 @@
-"""Train the learned tuner on the GB300 timing tables with the library's CUDA kernels, calibrate
-its confidence threshold on the training matrices, and evaluate it on the 200 held-out ones:
-mean / min fraction of the autotuner-best time, fallback rate, and the gain over the best
-fixed schedule (the one schedule with the best mean fraction on the training matrices).
+"""Train the learned tuners on the GB300 timing tables with the library's CUDA kernels, one
+network per value type, calibrate each network's confidence threshold, and evaluate it on the
+200 held-out matrices: mean / min fraction of the autotuner-best time, fallback rate, and the
+gain over the two methods without a network -- the best single fixed schedule (the one with
+the best mean fraction on the training matrices) and the library's fixed default schedule.
 
-    python -m benchmark_spmv_using_csr_gb300.tuner_data.train [timings.npz] [out_prefix]
+The threshold comes from matrices the network was not fitted on: a probe network is fitted on
+85 % of the training matrices and the threshold set on the other 15 % so that every probe pick
+below 95 % of the best time falls back to the sweep (with at most 25 % of matrices falling
+back); the final network is then fitted on all training matrices.
+
+    python -m benchmark_spmv_using_csr_gb300.tuner_data.train [data_dir] [value type name ...]
+
+Writes gb300_<name>_tuner.bin (the network file the C library reads) and
+gb300_<name>_report.json next to the timing files.
 """
 from __future__ import annotations
 
@@ -17,43 +26,60 @@ N_TRAIN = 2000
 EPOCHS, LR, WD = 300, 2e-3, 3e-4
 
 
-def main(data_path: str, out_prefix: str) -> dict:
+def _frac(ms, idx):
+    return ms.min(1) / ms[np.arange(len(ms)), idx]
+
+
+def train_one(data_dir: str, value_type: int) -> dict:
+    import benchmark_spmv_using_csr_gb300 as sp
     from benchmark_spmv_using_csr_gb300 import mlp
-    d = np.load(data_path)
+    name = sp.VALUE_NAMES[value_type]
+    d = np.load(os.path.join(data_dir, f"gb300_{name}_timings.npz"))
     done = int(d["done"])
-    f, ms = d["features"][:done], d["ms"][:done]
+    f, ms = d["features"][:done], d["ms"][:done].astype(np.float64)
+    cands = [tuple(int(v) for v in c) for c in d["candidates"]]
     ntr = min(N_TRAIN, done - max(done // 11, 1))
     ftr, mtr, fte, mte = f[:ntr], ms[:ntr], f[ntr:], ms[ntr:]
-    # the confidence threshold is calibrated on matrices the network was not fitted on: fit on
-    # 85 % of the training set, calibrate on the other 15 %, then refit on all of it
     nfit = int(0.85 * ntr)
-    cands = d["candidates"] if "candidates" in d.files else None
     probe = mlp.LearnedTuner(n_out=ms.shape[1], seed=0, candidates=cands)
     probe.fit(ftr[:nfit], mtr[:nfit], epochs=EPOCHS, batch=256, lr=LR, weight_decay=WD)
-    threshold = probe.calibrate_threshold(ftr[nfit:], mtr[nfit:], target=0.97, max_fallback=0.25)
+    threshold = probe.calibrate_threshold(ftr[nfit:], mtr[nfit:], floor=0.95, max_fallback=0.25)
+    validation = probe.evaluate(ftr[nfit:], mtr[nfit:])
     tuner = mlp.LearnedTuner(n_out=ms.shape[1], seed=0, candidates=cands)
     hist = tuner.fit(ftr, mtr, epochs=EPOCHS, batch=256, lr=LR, weight_decay=WD)
     tuner.threshold = threshold
     ev_te = tuner.evaluate(fte, mte)
     ev_tr = tuner.evaluate(ftr, mtr)
-    frac_tr = mtr.min(1, keepdims=True) / mtr
-    fixed = int(frac_tr.mean(0).argmax())
-    frac_fixed_te = mte.min(1) / mte[:, fixed]
-    report = {"train_matrices": int(ntr), "held_out_matrices": int(done - ntr),
+    fixed = int(np.nan_to_num(mtr.min(1, keepdims=True) / mtr).mean(0).argmax())
+    default = cands.index(tuple(sp.BhsparseSpmvCuda(value_type).get_config()))
+    frac_fixed = _frac(mte, np.full(len(mte), fixed))
+    frac_default = _frac(mte, np.full(len(mte), default))
+    report = {"value_type": name, "candidates": len(cands), "train_matrices": int(ntr),
+              "held_out_matrices": int(done - ntr),
               "final_train_loss": hist[-1], "first_train_loss": hist[0],
+              "validation_of_threshold": validation,
               "held_out": ev_te, "train": ev_tr,
-              "best_fixed_schedule": int(fixed),
-              "held_out_fixed_mean_frac_of_best": float(frac_fixed_te.mean()),
-              "held_out_fixed_min_frac_of_best": float(frac_fixed_te.min()),
-              "gain_over_fixed": float(ev_te["mean_frac_of_best"] / frac_fixed_te.mean())}
-    tuner.save(out_prefix + "_tuner.npz")
-    with open(out_prefix + "_report.json", "w") as fh:
+              "best_fixed_schedule": list(cands[fixed]),
+              "held_out_fixed_mean_frac_of_best": float(frac_fixed.mean()),
+              "held_out_fixed_min_frac_of_best": float(frac_fixed.min()),
+              "default_schedule": list(cands[default]),
+              "held_out_default_mean_frac_of_best": float(frac_default.mean()),
+              "gain_over_fixed": float(ev_te["mean_frac_of_best"] / frac_fixed.mean()),
+              "gain_over_default": float(ev_te["mean_frac_of_best"] / frac_default.mean())}
+    tuner.save(os.path.join(data_dir, f"gb300_{name}_tuner.bin"), value_type)
+    with open(os.path.join(data_dir, f"gb300_{name}_report.json"), "w") as fh:
         json.dump(report, fh, indent=1)
     return report
 
 
+def main(data_dir: str, names=None) -> dict:
+    import benchmark_spmv_using_csr_gb300 as sp
+    by_name = {v: k for k, v in sp.VALUE_NAMES.items()}
+    names = list(sp.VALUE_NAMES.values()) if not names else names
+    return {n: train_one(data_dir, by_name[n]) for n in names}
+
+
 if __name__ == "__main__":
     here = os.path.dirname(os.path.abspath(__file__))
-    data = sys.argv[1] if len(sys.argv) > 1 else os.path.join(here, "gb300_fp32_timings.npz")
-    prefix = sys.argv[2] if len(sys.argv) > 2 else os.path.join(here, "gb300_fp32")
-    print(json.dumps(main(data, prefix), indent=1))
+    data = sys.argv[1] if len(sys.argv) > 1 else here
+    print(json.dumps(main(data, sys.argv[2:]), indent=1))

@@ -86,10 +86,22 @@ int bhsp_set_device(bhsp_spmv* h, int device);
  * warps_per_cta 4 or 8, stages = 0 (each lane streams its values with 256-bit loads) or
  * 2 / 3 / 4 (values and column indices staged in a shared-memory ring of that many tiles by
  * 2D tensor copies; a matrix with no full tile runs the direct-load kernel).  Before
- * prepare_mem; 0 for seg / tiles_per_worker / warps_per_cta and -1 for stages keep the default
- * (16, 8, 4, 0; stages 2 for BHSP_VALUE_MIXED_BF16, whose staged schedule is the faster one).
- * Rejected if the staged ring does not fit in shared memory. */
+ * prepare_mem; 0 for seg / tiles_per_worker / warps_per_cta and -1 for stages take the fixed
+ * default (16, 8, 4, 0; stages 2 for BHSP_VALUE_MIXED_BF16, whose staged schedule is the faster
+ * one).  Rejected if the staged ring does not fit in shared memory.  Without this call
+ * prepare_mem chooses the schedule itself (bhsp_choose_schedule with the handle's network,
+ * see bhsp_set_tuner), which is what the reference's callers get: its geometry is a compile-
+ * time constant (spmv_cuda/common.h:39-48, spmv_cuda/bhsparse_spmv_cuda.h:323-328). */
 int bhsp_set_config(bhsp_spmv* h, int seg, int tiles_per_worker, int warps_per_cta, int stages);
+/* The network prepare_mem consults when bhsp_set_config was not called: NULL = the library's
+ * network for the handle's value type (the default; see bhsp_choose_schedule), "" = none (the
+ * fixed default schedule), else the path of a network file.  Before prepare_mem. */
+int bhsp_set_tuner(bhsp_spmv* h, const char* path);
+/* How prepare_mem chose the schedule in use: *source = one of BHSP_SCHEDULE_*, *confidence =
+ * the network's probability of its pick (0 when no network ran).  With the environment
+ * variable BHSP_LOG_SCHEDULE set (not "0"), prepare_mem also prints the schedule and its
+ * source to stderr, so a caller that cannot be changed shows what it got. */
+int bhsp_get_schedule_source(const bhsp_spmv* h, int* source, float* confidence);
 int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tiles_per_worker, int* warps_per_cta,
                     int* stages);
 /* Replace x (host pointer, same type as in prepare_mem) without rebuilding anything. */
@@ -205,18 +217,41 @@ void bhsp_batch_destroy(bhsp_batch* b);
 /* compile time: spmv_cuda/common.h:39-48).                                              */
 /* ------------------------------------------------------------------------------------ */
 /* The candidate schedules: index -> (non-zeros per lane, tiles per worker, warps per CTA,
- * stages). */
+ * stages): 24 direct-load schedules (S 8 / 16 / 32 x 1 / 4 / 8 / 16 tiles per worker x 4 / 8
+ * warps) and 8 TMA-staged ones (S 8 / 16 x 4 / 8 tiles per worker x 2 / 3 stages, 4 warps). */
 int bhsp_tune_num_candidates(void);
 int bhsp_tune_candidate(int index, int* seg, int* tiles_per_worker, int* warps_per_cta,
                         int* stages);
 /* Autotuner: validates the CSR, then times y = A.x for every candidate on the given device
  * buffers (`warmup` untimed runs, then the median of `reps` CUDA-event-timed runs, each
  * preceded by a write of twice the L2 size so that it starts with the matrix and x out of L2)
- * and writes ms_out[bhsp_tune_num_candidates()] and the index of the fastest to *best.
- * Synchronous. */
+ * and writes ms_out[bhsp_tune_num_candidates()] and the index of the fastest to *best.  A
+ * staged candidate whose ring does not fit in shared memory for this value type is not run and
+ * gets +infinity.  Synchronous. */
 int bhsp_autotune(int value_type, int m, int n, int nnz, const int* d_row_ptr,
                   const int* d_col_idx, const void* d_val, const void* d_x, void* d_y, int warmup,
                   int reps, float* ms_out, int* best, void* stream);
+/* Where a schedule came from (bhsp_choose_schedule, bhsp_get_schedule_source). */
+#define BHSP_SCHEDULE_CALLER 0  /* bhsp_set_config */
+#define BHSP_SCHEDULE_DEFAULT 1 /* the fixed default: no network for this value type */
+#define BHSP_SCHEDULE_LEARNED 2 /* the learned network's pick */
+#define BHSP_SCHEDULE_SWEEP 3   /* the full autotune sweep: the network was below its threshold */
+/* The schedule for a matrix held on the device: the 16 row features (bhsp_row_features) go
+ * through the learned network's forward kernels; its most probable candidate is taken when that
+ * probability reaches the network's calibrated confidence threshold, else the full autotune
+ * sweep (bhsp_autotune, 1 warm-up and the median of 3 flushed-L2 runs per candidate, writing
+ * d_y) decides.  tuner_path: NULL = the library's network for value_type, the file
+ * tuner_data/gb300_<f64|f32|mixed_f32|mixed_bf16>_tuner.bin next to the library (or in the
+ * directory named by the BHSP_TUNER_DIR environment variable); with no such file the fixed
+ * default is returned (*source = BHSP_SCHEDULE_DEFAULT).  "" = no network (the fixed default).
+ * Another path must name a network file trained for value_type.  The network only picks a
+ * schedule: every schedule computes the same y up to the summation order.  d_val / d_x / d_y
+ * are needed only by the sweep.  Synchronous. */
+int bhsp_choose_schedule(int value_type, int m, int n, int nnz, const int* d_row_ptr,
+                         const int* d_col_idx, const void* d_val, const void* d_x, void* d_y,
+                         const char* tuner_path, int* seg, int* tiles_per_worker,
+                         int* warps_per_cta, int* stages, int* source, float* confidence,
+                         void* stream);
 /* The 16 row-length statistics the learned tuner reads, computed on the device in one pass
  * over row_ptr:  0 log2(m+1), 1 log2(n+1), 2 log2(nnz+1), 3 log2(1+mean length),
  * 4 log2(1+std), 5 log2(1+max), 6 empty-row fraction, 7..15 fraction of rows whose length is

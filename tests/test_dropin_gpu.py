@@ -43,3 +43,22 @@ def test_benchmark_mode(binaries, use_double):
                        text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "PASS!" in r.stdout and "Bandwidth" in r.stdout
+
+
+def test_unchanged_caller_gets_a_tuned_schedule(binaries):
+    """The reference-style caller never sets a schedule; prepare_mem chooses one with the
+    library's learned network (or its sweep fallback) when a network file ships with the
+    library, which BHSP_LOG_SCHEDULE makes visible without touching the caller."""
+    from benchmark_spmv_using_csr_gb300.build import LIB_PATH
+    have_net = os.path.exists(os.path.join(os.path.dirname(LIB_PATH), "tuner_data",
+                                           "gb300_f64_tuner.bin"))
+    env = dict(os.environ, BHSP_LOG_SCHEDULE="1")
+    r = subprocess.run([binaries[1], "rand", "200000", "3"], capture_output=True, text=True,
+                       timeout=300, env=env)
+    assert r.returncode == 0 and "PASS!" in r.stdout, r.stdout + r.stderr
+    lines = [ln for ln in r.stderr.splitlines() if ln.startswith("bhsp: m=200000")]
+    assert lines, r.stderr
+    if have_net:
+        assert "the learned network" in lines[0] or "the autotune sweep" in lines[0], lines[0]
+    else:
+        assert "the fixed default" in lines[0], lines[0]

@@ -50,14 +50,128 @@ def test_training_learns_a_toy_rule(cuda_ok):
 
 
 DATA = os.path.join(os.path.dirname(mlp.__file__), "tuner_data")
+NAMES = ["f64", "f32", "mixed_f32", "mixed_bf16"]
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(DATA, "gb300_fp32_tuner.npz")),
-                    reason="no trained model committed")
-def test_committed_model_held_out(cuda_ok):
-    d = np.load(os.path.join(DATA, "gb300_fp32_timings.npz"))
+def _net_path(name):
+    return os.path.join(DATA, f"gb300_{name}_tuner.bin")
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_committed_network_on_device_kernels(cuda_ok, name):
+    """The committed network, run by the CUDA forward kernel, reproduces its held-out
+    evaluation: picks (with the sweep below the threshold) within 5 % of the autotuner-best
+    time on average."""
+    if not os.path.exists(_net_path(name)):
+        pytest.skip("no trained network committed")
+    d = np.load(os.path.join(DATA, f"gb300_{name}_timings.npz"))
     done = int(d["done"])
     f, ms = d["features"][:done], d["ms"][:done]
-    tuner = mlp.LearnedTuner.load(os.path.join(DATA, "gb300_fp32_tuner.npz"))
+    tuner = mlp.LearnedTuner.load(_net_path(name))
     ev = tuner.evaluate(f[2000:], ms[2000:])
     assert ev["mean_frac_of_best"] >= 0.95, ev
+    ref = mlp_oracle.forward(tuner.net.get_params(), f[2000:], tuner.net.mean, tuner.net.std,
+                             16, tuner.net.hidden, tuner.n_out)["p"]
+    np.testing.assert_allclose(tuner.net.forward(f[2000:]), ref, rtol=2e-4, atol=1e-6)
+
+
+def _write_with_threshold(src, dst, threshold):
+    d = mlp.read_network(src)
+    mlp.write_network(dst, d["value_type"], d["hidden"], threshold, d["mean"], d["std"],
+                      d["candidates"], d["params"])
+    return d
+
+
+def _prepare(vt, a, x, tuner=None):
+    import benchmark_spmv_using_csr_gb300 as sp
+    dt = sp.host_dtype(vt)
+    h = sp.BhsparseSpmvCuda(vt)
+    if tuner is not None:
+        assert h.set_tuner(tuner) == 0
+    y = np.zeros(a.m, dt)
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val.astype(dt), x.astype(dt), y) == 0, \
+        h.last_error
+    return h, y
+
+
+@pytest.mark.parametrize("vt", [0, 1, 2, 3])
+def test_prepare_mem_takes_the_networks_pick(cuda_ok, tmp_path, vt):
+    """Without bhsp_set_config, prepare_mem runs the learned network on the matrix's features
+    (forward kernel on the device) and takes its most probable schedule when the network is
+    confident: with the threshold set to 0 the schedule equals the argmax of the numpy
+    restatement of the network on the same features."""
+    import torch
+
+    import benchmark_spmv_using_csr_gb300 as sp
+    from benchmark_spmv_using_csr_gb300 import gen, tune
+    name = sp.VALUE_NAMES[vt]
+    if not os.path.exists(_net_path(name)):
+        pytest.skip("no trained network committed")
+    path = str(tmp_path / "net.bin")
+    d = _write_with_threshold(_net_path(name), path, 0.0)
+    for a in (gen.powerlaw(200_000, seed=3), gen.stencil3d(50, 40, 30, seed=4)):
+        x = gen.uniform(a.n, 5)
+        h, y = _prepare(vt, a, x, path)
+        src, conf = h.schedule_source()
+        assert src == sp.SCHEDULE_LEARNED
+        f = tune.row_features(torch.from_numpy(a.row_ptr).cuda(), a.n)
+        p = mlp_oracle.forward(d["params"], f[None], d["mean"], d["std"], 16, d["hidden"],
+                               d["n_out"])["p"][0]
+        assert tuple(h.get_config()) == tuple(int(v) for v in d["candidates"][p.argmax()])
+        assert abs(conf - p.max()) <= 1e-3
+        # the schedule only changes speed: y is the oracle's
+        assert h.run_benchmark() == 0 and h.get_y() == 0
+        if vt <= 1:
+            ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val.astype(y.dtype).astype(np.float64),
+                                    x.astype(y.dtype).astype(np.float64))
+            scale = oracle.csr_absrow(a.row_ptr, a.col, a.val.astype(y.dtype).astype(np.float64),
+                                      x.astype(y.dtype).astype(np.float64))
+            assert oracle.componentwise_error(y, ystar, scale) <= (1e-12 if vt == 0 else 1e-5)
+        h.close()
+
+
+def test_low_confidence_takes_the_sweep(cuda_ok, tmp_path):
+    """Below the network's confidence threshold prepare_mem runs the full autotune sweep; with
+    the threshold above any probability every matrix takes it."""
+    import benchmark_spmv_using_csr_gb300 as sp
+    from benchmark_spmv_using_csr_gb300 import gen, tune
+    if not os.path.exists(_net_path("f64")):
+        pytest.skip("no trained network committed")
+    path = str(tmp_path / "net.bin")
+    _write_with_threshold(_net_path("f64"), path, 2.0)
+    a = gen.powerlaw(100_000, seed=6)
+    x = gen.uniform(a.n, 7)
+    h, y = _prepare(sp.VALUE_F64, a, x, path)
+    src, conf = h.schedule_source()
+    assert src == sp.SCHEDULE_SWEEP and 0.0 < conf <= 1.0
+    assert tuple(h.get_config()) in tune.candidates()
+    # the sweep ran SpMVs into the device y; the caller's initial y is still what get_y returns
+    # before any run_benchmark, and run_benchmark gives the oracle's y
+    assert h.get_y() == 0 and not np.any(y)
+    assert h.run_benchmark() == 0 and h.get_y() == 0
+    ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)
+    scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, x)
+    assert oracle.componentwise_error(y, ystar, scale) <= 1e-12
+    h.close()
+
+
+def test_schedule_sources(cuda_ok):
+    import benchmark_spmv_using_csr_gb300 as sp
+    from benchmark_spmv_using_csr_gb300 import gen
+    a = gen.stencil2d(60, 50)
+    x = gen.uniform(a.n, 1)
+    h, _ = _prepare(sp.VALUE_F64, a, x, "")  # no network: the fixed default
+    assert h.schedule_source() == (sp.SCHEDULE_DEFAULT, 0.0)
+    assert tuple(h.get_config()) == sp.DEFAULT_CONFIG
+    h.close()
+    h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    assert h.set_config(8, 4, 4, 0) == 0
+    y = np.zeros(a.m)
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x, y) == 0
+    assert h.schedule_source()[0] == sp.SCHEDULE_CALLER and h.get_config() == (8, 4, 4, 0)
+    h.close()
+    h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    assert h.set_tuner("/nonexistent/net.bin") == 0
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x, y) == \
+        sp.BHSPARSE_INVALID_ARGUMENT
+    h.close()

@@ -5,11 +5,16 @@ from benchmark_spmv_using_csr_gb300 import gen, tune
 
 
 def test_candidate_table():
+    """24 direct-load schedules and 8 TMA-staged ones (stages 2 and 3 at S = 8 and 16)."""
     c = tune.candidates()
-    assert len(c) == 24
+    assert len(c) == 32
     assert len(set(c)) == len(c)
     for seg, tpw, warps, stages in c:
-        assert seg in (8, 16, 32) and tpw >= 1 and warps in (4, 8) and stages == 0
+        assert seg in (8, 16, 32) and tpw >= 1 and warps in (4, 8) and stages in (0, 2, 3)
+    staged = [x for x in c if x[3]]
+    assert len(staged) == 8 and {x[0] for x in staged} == {8, 16}
+    # the handle's default schedules are candidates (the trainer reports the gain over them)
+    assert (16, 8, 4, 0) in c and (16, 8, 4, 2) in c
 
 
 def _features_numpy(rp, n):
