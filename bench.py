@@ -299,19 +299,21 @@ def run_ours(args) -> None:
     x_pin = torch.from_numpy(x).pin_memory()
     y_pin = torch.zeros(a.m, dtype=torch.float64).pin_memory()
     y_np = y_pin.numpy()
-    tuning = None
-    if args.config is None:  # the autotuner picks the schedule on this matrix
-        tuning = autotune_workload(a, x)
-        args.config = tuning["pick"]
+    # the autotuner's full table on this matrix, for the report: the schedule itself is the one
+    # prepare_mem chooses (the learned network, or the sweep below its confidence threshold),
+    # as for any caller of the reference's API, unless --config sets one
+    tuning = autotune_workload(a, x)
     h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
-    assert h.set_config(*args.config) == 0, h.last_error
-    seg, tpw, warps, stages = h.get_config()
+    if args.config is not None:
+        assert h.set_config(*args.config) == 0, h.last_error
     assert h.set_device(local) == 0
     assert h.init_platform() == 0, h.last_error
     t_prep = time.perf_counter()
     rc = h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x_pin.numpy(), y_np)
     assert rc == 0, h.last_error
     t_prep = time.perf_counter() - t_prep
+    seg, tpw, warps, stages = h.get_config()
+    tuning["prepare_mem_choice"] = schedule_choice(h, tuning)
 
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
@@ -482,10 +484,9 @@ def run_ours(args) -> None:
 
 def measure_forms(args, a, x, ystar) -> dict:
     """The other value types on the same workload: device GB/s on their own algorithmic
-    bytes, non-zeros/s, and their error against the FP64 oracle.  Each form runs the faster
-    of its default schedule and the autotuner's pick for it (the autotuner's candidates load
-    the stream directly; BF16 storage defaults to the TMA-staged ring)."""
-    import numpy as np
+    bytes, non-zeros/s, and their error against the FP64 oracle.  Each form runs the schedule
+    its handle's prepare_mem chooses (that value type's learned network, or the sweep), shown
+    beside the autotuner's table for that value type."""
     import torch
 
     import benchmark_spmv_using_csr_gb300 as sp
@@ -494,18 +495,8 @@ def measure_forms(args, a, x, ystar) -> dict:
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
     steps = max(10, min(args.steps, 50))
     for vt, sv, sx in ((sp.VALUE_F32, 4, 4), (sp.VALUE_MIXED_F32, 4, 4), (sp.VALUE_MIXED_BF16, 2, 4)):
-        pick = tuple(autotune_workload(a, x, vt)["pick"])
-        dh = sp.BhsparseSpmvCuda(vt)
-        default = dh.get_config()
-        dh.close()
-        best = None
-        for cfg in dict.fromkeys((pick, default)):
-            r = _time_form(vt, cfg, a, x, flush, steps)
-            if "error" in r or best is None or r["ms"] < best[1]["ms"]:
-                best = (cfg, r)
-            if "error" in r:
-                break
-        cfg, r = best
+        tuning = autotune_workload(a, x, vt)
+        r = _time_form(vt, None, a, x, flush, steps, tuning)
         if "error" in r:
             out[sp.VALUE_NAMES[vt]] = {"error": r["error"]}
             continue
@@ -513,20 +504,23 @@ def measure_forms(args, a, x, ystar) -> dict:
         Bf = alg_bytes(a.m, a.n, a.nnz, sv, sx, 4)
         out[sp.VALUE_NAMES[vt]] = {
             "gbs": round(Bf / (ms * 1e-3) / 1e9, 1), "ms_per_step": round(ms, 5),
-            "gnnz_per_s": round(a.nnz / (ms * 1e-3) / 1e9, 2), "schedule": list(cfg),
+            "gnnz_per_s": round(a.nnz / (ms * 1e-3) / 1e9, 2), "schedule": r["choice"],
+            "autotuner_best": {"schedule": tuning["pick"], "ms": round(tuning["best_ms"], 5)},
             "normwise_err_vs_fp64_oracle": oracle.normwise_error(y, ystar)}
     return out
 
 
-def _time_form(vt, cfg, a, x, flush, steps) -> dict:
-    """Whole steps of one value type at one schedule through the handle (L2 flushed before
-    each, CUDA events): {"ms", "y"} or {"error"}."""
+def _time_form(vt, cfg, a, x, flush, steps, tuning=None) -> dict:
+    """Whole steps of one value type through the handle (L2 flushed before each, CUDA events),
+    at schedule cfg or, with cfg None, the one prepare_mem chooses: {"ms", "y", "choice"} or
+    {"error"}."""
     import numpy as np
     import torch
 
     import benchmark_spmv_using_csr_gb300 as sp
     h = sp.BhsparseSpmvCuda(vt)
-    assert h.set_config(*cfg) == 0, h.last_error
+    if cfg is not None:
+        assert h.set_config(*cfg) == 0, h.last_error
     dt = sp.host_dtype(vt)
     y = np.zeros(a.m, dt)
     if h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val.astype(dt), x.astype(dt), y):
@@ -549,25 +543,27 @@ def _time_form(vt, cfg, a, x, flush, steps) -> dict:
     assert h.check() == 0, h.last_error
     ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in evs)
     assert h.get_y() == 0
+    choice = schedule_choice(h, tuning)
     h.close()
-    return {"ms": ms, "y": y}
+    return {"ms": ms, "y": y, "choice": choice}
 
 
 def measure_fp64(args, a, x, config=None) -> dict:
     """Plain FP64 through the handle on one matrix: device GB/s per whole step (L2 flushed
-    before each, CUDA events), the schedule (autotuned unless given), and the componentwise
-    error against the FP64 compensated oracle."""
+    before each, CUDA events), the schedule (prepare_mem's choice unless given, beside the
+    autotuner's best), and the componentwise error against the FP64 compensated oracle."""
     import numpy as np
     import torch
 
     import benchmark_spmv_using_csr_gb300 as sp
     import oracle
-    tuning = autotune_workload(a, x) if config is None else None
-    cfg = tuning["pick"] if tuning else config
+    tuning = autotune_workload(a, x)
     h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
-    assert h.set_config(*cfg) == 0, h.last_error
+    if config is not None:
+        assert h.set_config(*config) == 0, h.last_error
     y = np.zeros(max(a.m, 1))
     assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x, y) == 0, h.last_error
+    choice = schedule_choice(h, tuning)
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
@@ -592,7 +588,8 @@ def measure_fp64(args, a, x, config=None) -> dict:
     h.close()
     return {"gbs": round(B / (ms * 1e-3) / 1e9, 1), "ms_per_step": round(ms, 5),
             "pct_of_peak": round(100 * B / (ms * 1e-3) / 1e9 / measured_peak()[0], 1),
-            "bytes_per_step": B, "schedule": list(cfg),
+            "bytes_per_step": B, "schedule": choice,
+            "autotuner_best": {"schedule": tuning["pick"], "ms": round(tuning["best_ms"], 5)},
             "componentwise_err_vs_fp64_oracle": err, "tolerance": 1e-12}
 
 
@@ -687,6 +684,22 @@ def cpu_openmp(a, x, B, seconds: float) -> dict:
     return out
 
 
+SOURCE_NAMES = {0: "caller (--config)", 1: "fixed default (no network)", 2: "learned network",
+                3: "autotune sweep (network below its confidence threshold)"}
+
+
+def schedule_choice(h, tuning) -> dict:
+    """The schedule prepare_mem chose, where it came from, and its time in the autotuner's table
+    as a fraction of the best."""
+    src, conf = h.schedule_source()
+    cfg = tuple(h.get_config())
+    key = ",".join(map(str, cfg))
+    t = tuning["table_ms"].get(key) if tuning else None
+    return {"schedule": list(cfg), "source": SOURCE_NAMES.get(src, str(src)),
+            "confidence": round(conf, 4),
+            "frac_of_autotuner_best": round(tuning["best_ms"] / t, 4) if t else None}
+
+
 def autotune_workload(a, x, vt=None) -> dict:
     """Run the library's autotuner (every candidate schedule, median of 11 timed runs, L2
     flushed before each) on the workload in value type vt (plain FP64 by default) and return
@@ -713,9 +726,9 @@ def autotune_workload(a, x, vt=None) -> dict:
 def measure_batched(args) -> dict:
     """The batched workload: 512 matrices (rows log-uniform in [1e3, 2e5], mixed generators),
     FP32 storage with compensated accumulation, k right-hand sides, one persistent kernel
-    replayed from a CUDA graph -- against the plain FP64 form launched once per matrix and
-    right-hand side (512*k sequential plain launches).  nnz*k per second, and the normwise
-    error of a subset of matrices against the FP64 oracle."""
+    replayed from a CUDA graph at the batched autotuner's pick -- against the plain FP64 form
+    launched once per matrix and right-hand side (512*k sequential plain launches).  nnz*k per
+    second, and the normwise error of a subset of matrices against the FP64 oracle."""
     import numpy as np
     import torch
 
@@ -724,6 +737,7 @@ def measure_batched(args) -> dict:
     from benchmark_spmv_using_csr_gb300 import batch, gen
     mats = gen.batch_workload(512)
     nnz = sum(a.nnz for a in mats)
+    mats_m, mats_n = sum(a.m for a in mats), sum(a.n for a in mats)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
 
     def timed(fn, reps):
@@ -761,10 +775,12 @@ def measure_batched(args) -> dict:
     del plans
     torch.cuda.empty_cache()
     for k in (1, 2, 4, 8):
-        b = batch.Batch(mats, k=k)
-        xh = gen.uniform(b.n * k, 3).reshape(b.n, k).astype(np.float32)
+        xh = gen.uniform(mats_n * k, 3).reshape(mats_n, k).astype(np.float32)
         xd = torch.from_numpy(xh).cuda()
-        yd = torch.zeros((b.m, k), dtype=torch.float32, device="cuda")
+        yd = torch.zeros((mats_m, k), dtype=torch.float32, device="cuda")
+        # the batched autotuner's pick for this k (its table, and the default schedule's time)
+        b, tb = batch.tuned(mats, k, xd, yd, reps=5)
+        dflt = ",".join(map(str, (32 if k == 4 else 16, 4, 4)))
         ms = timed(lambda: b.execute(xd, yd, use_graph=True), 10)
         b.check()
         ys, no = b.split(yd.cpu().numpy()), b.cat["n_off"]
@@ -776,10 +792,14 @@ def measure_batched(args) -> dict:
                 if np.linalg.norm(ystar) > 0:
                     worst = max(worst, oracle.normwise_error(ys[i][:, j], ystar))
         gk = nnz * k / ms / 1e6
+        info = b.info()
         out[f"k{k}"] = {"ms": round(ms, 4), "gnnz_k_per_s": round(gk, 2),
                         "vs_plain_fp64_sequential": round(ms_plain * k / ms, 2),
-                        "normwise_err_vs_fp64_oracle_max": worst, "launches": b.info()["launches"],
-                        "graph": True}
+                        "normwise_err_vs_fp64_oracle_max": worst, "launches": info["launches"],
+                        "graph": True, "schedule": tb["pick"],
+                        "variant": {"one_head": info["one_head"], "x_l2_only": info["x_l2_only"]},
+                        "default_schedule_ms": tb["table_ms"][dflt],
+                        "tuning_table_ms": tb["table_ms"]}
         b.close()
         del xd, yd
         torch.cuda.empty_cache()

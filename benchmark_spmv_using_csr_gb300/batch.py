@@ -60,6 +60,20 @@ class Batch:
         if rc != 0:
             raise RuntimeError(f"bhsp_batch_create failed with status {rc}")
 
+    def reschedule(self, seg: int, tiles_per_worker: int, warps_per_cta: int, stream=None) -> None:
+        """Rebuild the batch's plan at another schedule on the same device buffers."""
+        old = self._b
+        self._b = ctypes.c_void_p()
+        rc = lib().bhsp_batch_create(ctypes.byref(self._b), self.count, self.cat["m"],
+                                     self.cat["n"], self.cat["nnz"], self.row_ptr.data_ptr(),
+                                     self.col.data_ptr(), self.k, int(seg), int(tiles_per_worker),
+                                     int(warps_per_cta), ctypes.c_void_p(_stream_ptr(stream)))
+        if rc != 0:
+            self._b = old
+            raise RuntimeError(f"bhsp_batch_create failed with status {rc}")
+        if old:
+            lib().bhsp_batch_destroy(old)
+
     @property
     def m(self) -> int:
         return self.cat["m"]
@@ -87,7 +101,11 @@ class Batch:
     def info(self) -> dict:
         v = [ctypes.c_int() for _ in range(4)]
         lib().bhsp_batch_info(self._b, *[ctypes.byref(c) for c in v])
-        return dict(zip(("ntiles", "nworkers", "grid", "launches"), (c.value for c in v)))
+        out = dict(zip(("ntiles", "nworkers", "grid", "launches"), (c.value for c in v)))
+        oh, l2 = ctypes.c_int(), ctypes.c_int()
+        lib().bhsp_batch_variant(self._b, ctypes.byref(oh), ctypes.byref(l2))
+        out.update(one_head=bool(oh.value), x_l2_only=bool(l2.value))
+        return out
 
     @property
     def last_error(self) -> str:
@@ -108,3 +126,53 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def tune_candidates() -> list[tuple[int, int, int]]:
+    """(non-zeros per lane, tiles per worker, warps per CTA) of every batched candidate."""
+    L = lib()
+    out = []
+    for i in range(L.bhsp_batch_tune_num_candidates()):
+        v = [ctypes.c_int() for _ in range(3)]
+        assert L.bhsp_batch_tune_candidate(i, *[ctypes.byref(c) for c in v]) == 0
+        out.append(tuple(c.value for c in v))
+    return out
+
+
+def autotune(b: "Batch", x, y, warmup: int = 1, reps: int = 5, stream=None):
+    """Time every batched candidate schedule on the batch's matrices (graph replay, L2 flushed
+    before each timed run) with CUDA tensors x [n, k] and y [m, k]; returns (ms per candidate,
+    index of the fastest)."""
+    L = lib()
+    ms = np.zeros(L.bhsp_batch_tune_num_candidates(), np.float32)
+    best = ctypes.c_int(-1)
+    rc = L.bhsp_batch_autotune(b.count, b.m, b.n, b.nnz, b.row_ptr.data_ptr(), b.col.data_ptr(),
+                               b.k, b.val.data_ptr(), x.data_ptr(), y.data_ptr(), int(warmup),
+                               int(reps), ms.ctypes.data_as(ctypes.c_void_p), ctypes.byref(best),
+                               ctypes.c_void_p(_stream_ptr(stream)))
+    if rc != 0:
+        raise RuntimeError(f"bhsp_batch_autotune failed with status {rc}")
+    return ms, best.value
+
+
+def tuned(mats, k: int, x, y, cache=None, reps: int = 5):
+    """A Batch at the schedule the batched autotuner picks for these matrices and k (looked up
+    in, or added to, a tune.TuneCache keyed by k and the concatenated matrix's row features).
+    Returns (batch, {"pick", "ms", "table", "cached"})."""
+    from . import tune
+    b = Batch(mats, k=k)
+    key_vt = 100 + int(k)  # cache namespace of the batched form at k right-hand sides
+    feats = tune.row_features(b.row_ptr, b.n)
+    hit = cache.get(key_vt, feats) if cache is not None else None
+    if hit is not None:
+        ms, best = hit
+    else:
+        ms, best = autotune(b, x, y, reps=reps)
+        if cache is not None:
+            cache.put(key_vt, feats, ms, best)
+            cache.save()
+    cands = tune_candidates()
+    b.reschedule(*cands[best])
+    return b, {"pick": list(cands[best]), "ms": float(ms[best]),
+                "table_ms": {",".join(map(str, c)): round(float(t), 4) for c, t in zip(cands, ms)},
+                "cached": hit is not None}

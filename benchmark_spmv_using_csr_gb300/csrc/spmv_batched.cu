@@ -11,6 +11,7 @@
 // uneven matrices load-balance over the SMs; the calibration kernel then adds the carry
 // records.  The ticket reset, the persistent kernel and the calibration are captured once in a
 // CUDA graph and replayed by every call.
+#include <algorithm>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -60,6 +61,34 @@ __device__ __forceinline__ VecF<4> ld_x(const VecF<4>* p, uint64_t) {
 __device__ __forceinline__ VecF<8> ld_x(const VecF<8>* p, uint64_t) {
     VecF<8> r;
     asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]), "=f"(r.v[4]),
+                   "=f"(r.v[5]), "=f"(r.v[6]), "=f"(r.v[7])
+                 : "l"(p));
+    return r;
+}
+
+// the same gathers from L2 only (ld.global.cg), the batch's plan choice when its columns have no
+// locality
+__device__ __forceinline__ VecF<1> ld_x_l2(const VecF<1>* p) {
+    VecF<1> r;
+    asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(r.v[0]) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ VecF<2> ld_x_l2(const VecF<2>* p) {
+    VecF<2> r;
+    asm volatile("ld.global.cg.v2.f32 {%0,%1}, [%2];" : "=f"(r.v[0]), "=f"(r.v[1]) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ VecF<4> ld_x_l2(const VecF<4>* p) {
+    VecF<4> r;
+    asm volatile("ld.global.cg.v4.f32 {%0,%1,%2,%3}, [%4];"
+                 : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3])
+                 : "l"(p));
+    return r;
+}
+__device__ __forceinline__ VecF<8> ld_x_l2(const VecF<8>* p) {
+    VecF<8> r;
+    asm volatile("ld.global.cg.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]), "=f"(r.v[4]),
                    "=f"(r.v[5]), "=f"(r.v[6]), "=f"(r.v[7])
                  : "l"(p));
@@ -169,38 +198,37 @@ struct PolMixedK {
     }
 };
 
-// the persistent kernel for K right-hand sides: register-capped from 4 on
-template <int K, int S, int WARPS>
+// the persistent kernel for K right-hand sides: register-capped from 4 on.  OH (the one-head
+// chunk form) exists for one right-hand side only, whose accumulator is scalar.
+template <int K, int S, int WARPS, bool OH, bool XL2>
 constexpr auto persistent_kernel() {
     if constexpr (K >= 4)
-        return &k_tiles_persistent_capped<PolMixedK<K>, S, WARPS>;
+        return &k_tiles_persistent_capped<PolMixedK<K>, S, WARPS, false, XL2>;
     else
-        return &k_tiles_persistent<PolMixedK<K>, S, WARPS>;
+        return &k_tiles_persistent<PolMixedK<K>, S, WARPS, OH && K == 1, XL2>;
 }
 
-template <int K, int S, int WARPS>
+template <int K, int S, int WARPS, bool OH, bool XL2>
 static cudaError_t enqueue_batched(const TileArgs<PolMixedK<K>>& a, int tpw, int nworkers,
                                    int ntiles, int* ticket, int grid, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
     if (nworkers > 0)
-        persistent_kernel<K, S, WARPS>()<<<grid, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles,
-                                                                     ticket);
+        persistent_kernel<K, S, WARPS, OH, XL2>()<<<grid, WARPS * 32, 0, st>>>(a, tpw, nworkers,
+                                                                               ntiles, ticket);
     const int cb = grid_for(nworkers, 256, 8);
     k_calibrate<PolMixedK<K>><<<cb, 256, 0, st>>>(a.rec_row, a.rec_val, nworkers, a.y, a.tile_ptr,
                                                   a.m, a.err);
     return cudaGetLastError();
 }
 
-template <int K, int S, int WARPS>
+template <int K, int S, int WARPS, bool OH, bool XL2>
 static int persistent_grid() {
-    int dev = 0, sms = 0, per_sm = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, persistent_kernel<K, S, WARPS>(), WARPS * 32, 0) != cudaSuccess)
+            &per_sm, persistent_kernel<K, S, WARPS, OH, XL2>(), WARPS * 32, 0) != cudaSuccess)
         return 0;
-    return sms * (per_sm > 0 ? per_sm : 1);
+    return device_sm_count() * (per_sm > 0 ? per_sm : 1);
 }
 
 struct BatchLaunch {
@@ -217,7 +245,14 @@ struct BatchLaunch {
     int m, n, nnz;
 };
 
-template <int K, int S, int WARPS>
+// The plan's kernel variant: the one-head chunk form (one right-hand side, few short rows) and
+// L2-only x gathers (columns without locality), both chosen from counts made on the device.
+struct BatchVariant {
+    bool one_head = false;
+    bool x_l2 = false;
+};
+
+template <int K, int S, int WARPS, bool OH, bool XL2>
 static cudaError_t enqueue_k(const BatchLaunch& l, int tpw, int grid, cudaStream_t st) {
     TileArgs<PolMixedK<K>> a;
     a.row_ptr = l.row_ptr;
@@ -235,50 +270,66 @@ static cudaError_t enqueue_k(const BatchLaunch& l, int tpw, int grid, cudaStream
     a.phase = 3;
     const int nt = num_tiles(l.nnz, 32 * S);
     const int nw = (nt + tpw - 1) / tpw;
-    return enqueue_batched<K, S, WARPS>(a, tpw, nw, nt, l.ticket, grid, st);
+    return enqueue_batched<K, S, WARPS, OH, XL2>(a, tpw, nw, nt, l.ticket, grid, st);
 }
 
-// dispatch over k (1,2,4,8) x S (8,16,32) x warps (4,8)
-#define SPMV_BATCH_DISPATCH(FN, K, ...)                                                     \
-    switch (K) {                                                                            \
-        case 1: return FN<1>(__VA_ARGS__);                                                  \
-        case 2: return FN<2>(__VA_ARGS__);                                                  \
-        case 4: return FN<4>(__VA_ARGS__);                                                  \
-        case 8: return FN<8>(__VA_ARGS__);                                                  \
-        default: return cudaErrorInvalidValue;                                              \
-    }
-
+// dispatch over the variant (one-head form for k = 1 only, L2-only gathers), then S and warps
+template <int K, int S, int WARPS>
+static cudaError_t enqueue_v(const BatchLaunch& l, const BatchVariant& v, int tpw, int grid,
+                             cudaStream_t st) {
+    if (K == 1 && v.one_head)
+        return v.x_l2 ? enqueue_k<K, S, WARPS, true, true>(l, tpw, grid, st)
+                      : enqueue_k<K, S, WARPS, true, false>(l, tpw, grid, st);
+    return v.x_l2 ? enqueue_k<K, S, WARPS, false, true>(l, tpw, grid, st)
+                  : enqueue_k<K, S, WARPS, false, false>(l, tpw, grid, st);
+}
 template <int K>
-static cudaError_t enqueue_any(const BatchLaunch& l, const TileConfig& c, int grid, cudaStream_t st) {
+static cudaError_t enqueue_any(const BatchLaunch& l, const TileConfig& c, const BatchVariant& v,
+                               int grid, cudaStream_t st) {
     const bool w8 = c.warps_per_cta == 8;
+    const int tpw = c.tiles_per_worker;
     switch (c.seg) {
-        case 8: return w8 ? enqueue_k<K, 8, 8>(l, c.tiles_per_worker, grid, st) : enqueue_k<K, 8, 4>(l, c.tiles_per_worker, grid, st);
-        case 16: return w8 ? enqueue_k<K, 16, 8>(l, c.tiles_per_worker, grid, st) : enqueue_k<K, 16, 4>(l, c.tiles_per_worker, grid, st);
-        case 32: return w8 ? enqueue_k<K, 32, 8>(l, c.tiles_per_worker, grid, st) : enqueue_k<K, 32, 4>(l, c.tiles_per_worker, grid, st);
+        case 8: return w8 ? enqueue_v<K, 8, 8>(l, v, tpw, grid, st) : enqueue_v<K, 8, 4>(l, v, tpw, grid, st);
+        case 16: return w8 ? enqueue_v<K, 16, 8>(l, v, tpw, grid, st) : enqueue_v<K, 16, 4>(l, v, tpw, grid, st);
+        case 32: return w8 ? enqueue_v<K, 32, 8>(l, v, tpw, grid, st) : enqueue_v<K, 32, 4>(l, v, tpw, grid, st);
         default: return cudaErrorInvalidValue;
     }
 }
-static cudaError_t enqueue_batch(const BatchLaunch& l, int k, const TileConfig& c, int grid,
-                                 cudaStream_t st) {
-    SPMV_BATCH_DISPATCH(enqueue_any, k, l, c, grid, st)
+static cudaError_t enqueue_batch(const BatchLaunch& l, int k, const TileConfig& c,
+                                 const BatchVariant& v, int grid, cudaStream_t st) {
+    switch (k) {
+        case 1: return enqueue_any<1>(l, c, v, grid, st);
+        case 2: return enqueue_any<2>(l, c, v, grid, st);
+        case 4: return enqueue_any<4>(l, c, v, grid, st);
+        case 8: return enqueue_any<8>(l, c, v, grid, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
+template <int K, int S, int WARPS>
+static int grid_v(const BatchVariant& v) {
+    if (K == 1 && v.one_head)
+        return v.x_l2 ? persistent_grid<K, S, WARPS, true, true>()
+                      : persistent_grid<K, S, WARPS, true, false>();
+    return v.x_l2 ? persistent_grid<K, S, WARPS, false, true>()
+                  : persistent_grid<K, S, WARPS, false, false>();
+}
 template <int K>
-static int grid_any(const TileConfig& c) {
+static int grid_any(const TileConfig& c, const BatchVariant& v) {
     const bool w8 = c.warps_per_cta == 8;
     switch (c.seg) {
-        case 8: return w8 ? persistent_grid<K, 8, 8>() : persistent_grid<K, 8, 4>();
-        case 16: return w8 ? persistent_grid<K, 16, 8>() : persistent_grid<K, 16, 4>();
-        case 32: return w8 ? persistent_grid<K, 32, 8>() : persistent_grid<K, 32, 4>();
+        case 8: return w8 ? grid_v<K, 8, 8>(v) : grid_v<K, 8, 4>(v);
+        case 16: return w8 ? grid_v<K, 16, 8>(v) : grid_v<K, 16, 4>(v);
+        case 32: return w8 ? grid_v<K, 32, 8>(v) : grid_v<K, 32, 4>(v);
         default: return 0;
     }
 }
-static int batch_grid(int k, const TileConfig& c) {
+static int batch_grid(int k, const TileConfig& c, const BatchVariant& v) {
     switch (k) {
-        case 1: return grid_any<1>(c);
-        case 2: return grid_any<2>(c);
-        case 4: return grid_any<4>(c);
-        case 8: return grid_any<8>(c);
+        case 1: return grid_any<1>(c, v);
+        case 2: return grid_any<2>(c, v);
+        case 4: return grid_any<4>(c, v);
+        case 8: return grid_any<8>(c, v);
         default: return 0;
     }
 }
@@ -291,6 +342,8 @@ struct bhsp_batch {
     int count = 0, k = 1;
     int m = 0, n = 0, nnz = 0;  // totals of the concatenated block-diagonal matrix
     TileConfig cfg{};
+    BatchVariant var{};
+    int short_rows = 0, x_sampled = 0, x_near = 0;  // the counts the variant came from
     int ntiles = 0, nworkers = 0, grid = 0;
     const int* row_ptr = nullptr;
     const int* col = nullptr;
@@ -358,10 +411,30 @@ extern "C" int bhsp_batch_create(bhsp_batch** out, int count, int m_total, int n
     b->col = d_col_idx;
     b->ntiles = num_tiles(nnz_total, 32 * c.seg);
     b->nworkers = (b->ntiles + c.tiles_per_worker - 1) / c.tiles_per_worker;
-    b->grid = batch_grid(k, c);
     cudaError_t e = cudaSuccess;
+    {
+        // the kernel variant, as for a single matrix's plan: short rows against the chunk
+        // width of the batched kernel, and the locality of about 2^20 sampled columns
+        const int cw = k == 8 ? 2 : (c.seg == 8 || k == 4) ? 4 : 8;  // chunk_width<S, x entry>
+        const int step = nnz_total > (1 << 20) ? nnz_total / (1 << 20) : 1;
+        uint32_t* counts = nullptr;
+        uint32_t h[3] = {0u, 0u, 0u};
+        e = cudaMalloc(&counts, 3 * sizeof(uint32_t));
+        if (e == cudaSuccess) e = launch_short_rows(d_row_ptr, m_total, cw, counts, st);
+        if (e == cudaSuccess)
+            e = launch_x_locality(d_row_ptr, d_col_idx, m_total, nnz_total, step, counts + 1, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, counts, sizeof h, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaFree(counts);
+        b->short_rows = (int)h[0];
+        b->x_sampled = (int)h[1];
+        b->x_near = (int)h[2];
+        b->var.one_head = k == 1 && one_head_pays(h[0], nnz_total, cw);
+        b->var.x_l2 = x_l2_pays(h[1], h[2]);
+    }
+    b->grid = e == cudaSuccess ? batch_grid(k, c, b->var) : 0;
     const size_t nw = b->nworkers > 0 ? (size_t)b->nworkers : 1;
-    if (b->grid <= 0) e = cudaErrorInvalidConfiguration;
+    if (e == cudaSuccess && b->grid <= 0) e = cudaErrorInvalidConfiguration;
     if (e == cudaSuccess) e = cudaMalloc(&b->tile_ptr, sizeof(uint32_t) * ((size_t)b->ntiles + 1));
     if (e == cudaSuccess) e = cudaMalloc(&b->rec_row, sizeof(int) * nw);
     if (e == cudaSuccess) e = cudaMalloc(&b->rec_val, sizeof(double) * k * nw);
@@ -407,7 +480,7 @@ extern "C" int bhsp_batch_execute(bhsp_batch* b, const float* d_val, const float
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const BatchLaunch l = batch_launch(b, d_val, d_x, d_y);
     if (!use_graph) {
-        cudaError_t e = enqueue_batch(l, b->k, b->cfg, b->grid, st);
+        cudaError_t e = enqueue_batch(l, b->k, b->cfg, b->var, b->grid, st);
         return e == cudaSuccess ? BHSPARSE_SUCCESS : batch_cuda(b, e, "batched launch");
     }
     if (!b->exec || b->g_val != d_val || b->g_x != d_x || b->g_y != d_y) {
@@ -421,7 +494,7 @@ extern "C" int bhsp_batch_execute(bhsp_batch* b, const float* d_val, const float
         if (e != cudaSuccess) return batch_cuda(b, e, "capture stream");
         e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaError_t e2 = enqueue_batch(l, b->k, b->cfg, b->grid, cs);
+            cudaError_t e2 = enqueue_batch(l, b->k, b->cfg, b->var, b->grid, cs);
             e = cudaStreamEndCapture(cs, &b->graph);
             if (e == cudaSuccess) e = e2;
         }
@@ -472,4 +545,98 @@ extern "C" void bhsp_batch_destroy(bhsp_batch* b) {
     if (!b) return;
     batch_release(b);
     delete b;
+}
+
+extern "C" int bhsp_batch_variant(const bhsp_batch* b, int* one_head, int* l2_only) {
+    if (!b) return BHSPARSE_INVALID_ARGUMENT;
+    if (one_head) *one_head = b->var.one_head ? 1 : 0;
+    if (l2_only) *l2_only = b->var.x_l2 ? 1 : 0;
+    return BHSPARSE_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------------------
+// Schedule tuner of the batched form
+// ---------------------------------------------------------------------------------------
+namespace {
+struct BatchCand {
+    int seg, tpw, warps;
+};
+// S in {8, 16, 32} x tiles per worker in {1, 2, 4, 8} x warps per CTA in {4, 8}
+const BatchCand kBatchCands[] = {
+    {8, 1, 4},  {8, 1, 8},  {8, 2, 4},  {8, 2, 8},  {8, 4, 4},  {8, 4, 8},  {8, 8, 4},  {8, 8, 8},
+    {16, 1, 4}, {16, 1, 8}, {16, 2, 4}, {16, 2, 8}, {16, 4, 4}, {16, 4, 8}, {16, 8, 4}, {16, 8, 8},
+    {32, 1, 4}, {32, 1, 8}, {32, 2, 4}, {32, 2, 8}, {32, 4, 4}, {32, 4, 8}, {32, 8, 4}, {32, 8, 8},
+};
+constexpr int kNumBatchCands = sizeof(kBatchCands) / sizeof(kBatchCands[0]);
+}  // namespace
+
+extern "C" int bhsp_batch_tune_num_candidates(void) { return kNumBatchCands; }
+
+extern "C" int bhsp_batch_tune_candidate(int index, int* seg, int* tiles_per_worker,
+                                         int* warps_per_cta) {
+    if (index < 0 || index >= kNumBatchCands) return BHSPARSE_INVALID_ARGUMENT;
+    if (seg) *seg = kBatchCands[index].seg;
+    if (tiles_per_worker) *tiles_per_worker = kBatchCands[index].tpw;
+    if (warps_per_cta) *warps_per_cta = kBatchCands[index].warps;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_batch_autotune(int count, int m_total, int n_total, int nnz_total,
+                                   const int* d_row_ptr, const int* d_col_idx, int k,
+                                   const float* d_val, const float* d_x, float* d_y, int warmup,
+                                   int reps, float* ms_out, int* best, void* stream) {
+    if (warmup < 0 || reps < 1 || !ms_out) return BHSPARSE_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return BHSPARSE_CUDA_ERROR;
+    }
+    // a write of twice the L2 size before every timed run (skipped if it cannot be allocated)
+    void* flush = nullptr;
+    size_t flush_bytes = 0;
+    int dev = 0, l2 = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) == cudaSuccess && l2 > 0) {
+        flush_bytes = 2 * (size_t)l2;
+        if (cudaMalloc(&flush, flush_bytes) != cudaSuccess) {
+            flush = nullptr;
+            cudaGetLastError();
+        }
+    }
+    int rc = BHSPARSE_SUCCESS, best_i = -1;
+    float best_ms = 0.f;
+    std::vector<float> t((size_t)reps);
+    for (int i = 0; i < kNumBatchCands && rc == BHSPARSE_SUCCESS; ++i) {
+        bhsp_batch* b = nullptr;
+        rc = bhsp_batch_create(&b, count, m_total, n_total, nnz_total, d_row_ptr, d_col_idx, k,
+                               kBatchCands[i].seg, kBatchCands[i].tpw, kBatchCands[i].warps,
+                               stream);
+        if (rc) break;
+        for (int w = 0; w < warmup && rc == 0; ++w) rc = bhsp_batch_execute(b, d_val, d_x, d_y, 1, stream);
+        for (int r = 0; r < reps && rc == 0; ++r) {
+            if (flush && cudaMemsetAsync(flush, r & 0xff, flush_bytes, st) != cudaSuccess)
+                rc = BHSPARSE_CUDA_ERROR;
+            if (!rc && cudaEventRecord(e0, st) != cudaSuccess) rc = BHSPARSE_CUDA_ERROR;
+            if (!rc) rc = bhsp_batch_execute(b, d_val, d_x, d_y, 1, stream);
+            if (!rc && cudaEventRecord(e1, st) != cudaSuccess) rc = BHSPARSE_CUDA_ERROR;
+            if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = BHSPARSE_CUDA_ERROR;
+            if (!rc && cudaEventElapsedTime(&t[(size_t)r], e0, e1) != cudaSuccess)
+                rc = BHSPARSE_CUDA_ERROR;
+        }
+        if (!rc) rc = bhsp_batch_check(b, stream);
+        bhsp_batch_destroy(b);
+        if (rc) break;
+        std::sort(t.begin(), t.end());
+        ms_out[i] = t[(size_t)reps / 2];
+        if (best_i < 0 || ms_out[i] < best_ms) {
+            best_i = i;
+            best_ms = ms_out[i];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (flush) cudaFree(flush);
+    if (best) *best = best_i;
+    return rc;
 }

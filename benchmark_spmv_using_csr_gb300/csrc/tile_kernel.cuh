@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
 // worker index from a global ticket until none is left (the global tile work queue of the
 // batched form: workers are consecutive tile ranges, so the ticket walks the tiles in order).
 // The persistent loop: each warp takes the next worker index from the ticket until none is left.
-template <class P, int S>
+template <class P, int S, bool OH, bool XL2>
 __device__ __forceinline__ void persistent_workers(const TileArgs<P>& a, int tpw, int nworkers,
                                                    int ntiles, int* ticket, uint32_t* s_words_w,
                                                    int* rowof) {
@@ -614,18 +614,20 @@ __device__ __forceinline__ void persistent_workers(const TileArgs<P>& a, int tpw
             if (lane == 0) atomicOr(a.err, ERR_QUEUE);
             break;
         }
-        tile_worker<P, S>(a, w, tpw, ntiles, s_words_w, rowof);
+        tile_worker<P, S, OH, false, XL2>(a, w, tpw, ntiles, s_words_w, rowof);
         __syncwarp();
     }
 }
 
-template <class P, int S, int WARPS>
+// OH / XL2: the plan's chunk form and x gather path, as for k_tiles (fixed per batch)
+template <class P, int S, int WARPS, bool OH, bool XL2>
 __global__ void __launch_bounds__(WARPS * 32)
     k_tiles_persistent(TileArgs<P> a, int tpw, int nworkers, int ntiles, int* ticket) {
     __shared__ uint32_t s_words[WARPS][32];
     __shared__ int s_rowof[WARPS][32 * S];
     const int warp = threadIdx.x >> 5;
-    persistent_workers<P, S>(a, tpw, nworkers, ntiles, ticket, s_words[warp], s_rowof[warp]);
+    persistent_workers<P, S, OH, XL2>(a, tpw, nworkers, ntiles, ticket, s_words[warp],
+                                      s_rowof[warp]);
 }
 
 // The same with 16 resident warps per SM asked of the register allocator (128 registers), for
@@ -633,13 +635,14 @@ __global__ void __launch_bounds__(WARPS * 32)
 // right-hand sides take 148 registers and 12 warps uncapped, a 48-byte spill capped).  One and
 // two right-hand sides keep the uncapped kernel: any explicit minimum changed their code and
 // cost one right-hand side 3-14 %.
-template <class P, int S, int WARPS>
+template <class P, int S, int WARPS, bool OH, bool XL2>
 __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
     k_tiles_persistent_capped(TileArgs<P> a, int tpw, int nworkers, int ntiles, int* ticket) {
     __shared__ uint32_t s_words[WARPS][32];
     __shared__ int s_rowof[WARPS][32 * S];
     const int warp = threadIdx.x >> 5;
-    persistent_workers<P, S>(a, tpw, nworkers, ntiles, ticket, s_words[warp], s_rowof[warp]);
+    persistent_workers<P, S, OH, XL2>(a, tpw, nworkers, ntiles, ticket, s_words[warp],
+                                      s_rowof[warp]);
 }
 
 // Exchange of any carry-record type between lanes (as 32-bit words).

@@ -209,6 +209,22 @@ int bhsp_batch_execute(bhsp_batch* b, const float* d_val, const float* d_x, floa
                        int use_graph, void* stream);
 int bhsp_batch_check(bhsp_batch* b, void* stream);
 int bhsp_batch_info(const bhsp_batch* b, int* ntiles, int* nworkers, int* grid, int* launches);
+/* The kernel variant bhsp_batch_create chose for the batch, as bhsp_plan_chunk_form /
+ * bhsp_plan_gather_path do for one matrix: *one_head = 1 for the branch-free one-head chunk form
+ * (one right-hand side and few rows shorter than a chunk), *l2_only = 1 when x is gathered from
+ * L2 only (fewer than half of about 2^20 sampled columns lie near their neighbours). */
+int bhsp_batch_variant(const bhsp_batch* b, int* one_head, int* l2_only);
+/* The batched form's schedule tuner.  Candidates: S 8 / 16 / 32 x 1 / 2 / 4 / 8 tiles per
+ * worker x 4 / 8 warps per CTA.  bhsp_batch_autotune builds the batch at every candidate and
+ * times bhsp_batch_execute (graph replay; `warmup` untimed runs, then the median of `reps`
+ * CUDA-event-timed runs, each after a write of twice the L2 size) on the caller's buffers,
+ * writing ms_out[bhsp_batch_tune_num_candidates()] and the fastest's index to *best; pass the
+ * pick to bhsp_batch_create.  Synchronous. */
+int bhsp_batch_tune_num_candidates(void);
+int bhsp_batch_tune_candidate(int index, int* seg, int* tiles_per_worker, int* warps_per_cta);
+int bhsp_batch_autotune(int count, int m_total, int n_total, int nnz_total, const int* d_row_ptr,
+                        const int* d_col_idx, int k, const float* d_val, const float* d_x,
+                        float* d_y, int warmup, int reps, float* ms_out, int* best, void* stream);
 const char* bhsp_batch_last_error(const bhsp_batch* b);
 void bhsp_batch_destroy(bhsp_batch* b);
 

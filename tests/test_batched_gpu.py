@@ -80,3 +80,54 @@ def test_graph_replay_equals_direct_and_is_stable(cuda_ok):
     info = b.info()
     assert info["launches"] == 2 and info["grid"] >= 152
     b.close()
+
+
+@pytest.mark.parametrize("k", [1, 8])
+def test_batched_autotune_pick_is_correct_and_no_slower(cuda_ok, tmp_path, k):
+    """The batched autotuner times every candidate schedule; its pick is the fastest of the
+    table, so at least as fast as the default schedule (which is a candidate), gives y within
+    the mixed form's tolerance, and a second call takes the cached table."""
+    import torch
+    from benchmark_spmv_using_csr_gb300 import tune
+    mats = _mats(13, count=40)
+    b0 = batch.Batch(mats, k=k)
+    x_np = gen.uniform(b0.n * k, 4).reshape(b0.n, k)
+    x = torch.from_numpy(x_np.astype(np.float32)).cuda()
+    y = torch.zeros((b0.m, k), dtype=torch.float32, device="cuda")
+    b0.close()
+    cache = tune.TuneCache(str(tmp_path / "batch.json"))
+    b, t = batch.tuned(mats, k, x, y, cache=cache, reps=3)
+    cands = batch.tune_candidates()
+    ms = np.array([t["table_ms"][",".join(map(str, c))] for c in cands])
+    assert np.all(ms > 0) and tuple(t["pick"]) == cands[int(np.argmin(ms))]
+    dflt = (32 if k == 4 else 16, 4, 4)
+    assert dflt in cands and ms.min() <= ms[cands.index(dflt)]
+    y.fill_(float("nan"))
+    b.execute(x, y)
+    b.check()
+    ys = b.split(y.cpu().numpy())
+    no = b.cat["n_off"]
+    for i, a in enumerate(mats):
+        for j in range(k):
+            ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x_np[no[i]:no[i + 1], j].copy())
+            if np.linalg.norm(ystar) > 0:
+                assert oracle.normwise_error(ys[i][:, j].astype(np.float64), ystar) <= TOL_MIXED_NORMWISE
+    b.close()
+    b2, t2 = batch.tuned(mats, k, x, y, cache=cache)
+    assert t2["cached"] and t2["pick"] == t["pick"]
+    b2.close()
+
+
+def test_batched_variant_follows_the_columns(cuda_ok):
+    """The batch's kernel variant comes from the same counts as a single matrix's plan: random
+    columns gather from L2 only, stencils through L1; the one-head form only at k = 1."""
+    dense_random = [gen.density(20_000, 20_000, 1e-3, seed=s) for s in range(4)]
+    stencils = [gen.stencil3d(20, 20, 20, seed=s) for s in range(4)]
+    b = batch.Batch(dense_random, k=1)
+    assert b.info()["x_l2_only"]
+    b.close()
+    for k in (1, 2):
+        b = batch.Batch(stencils, k=k)
+        info = b.info()
+        assert not info["x_l2_only"] and info["one_head"] == (k == 1)
+        b.close()
