@@ -7,6 +7,7 @@ import os
 import numpy as np
 import pytest
 
+import oracle
 from oracle import mlp_oracle
 from benchmark_spmv_using_csr_gb300 import mlp
 
