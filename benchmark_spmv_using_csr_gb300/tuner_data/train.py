@@ -1,13 +1,13 @@
 """Train the learned tuners on the GB300 timing tables with the library's CUDA kernels, one
 network per value type, calibrate each network's confidence threshold, and evaluate it on the
-200 held-out matrices: mean / min fraction of the autotuner-best time, fallback rate, and the
+220 held-out matrices (see split): mean / min fraction of the autotuner-best time, fallback rate, and the
 gain over the two methods without a network -- the best single fixed schedule (the one with
 the best mean fraction on the training matrices) and the library's fixed default schedule.
 
 The threshold comes from matrices the network was not fitted on: a probe network is fitted on
-85 % of the training matrices and the threshold set on the other 15 % so that every probe pick
-below 95 % of the best time falls back to the sweep (with at most 25 % of matrices falling
-back); the final network is then fitted on all training matrices.
+6 of every 7 training matrices and the threshold set on the 7th so that every probe pick below
+95 % of the best time falls back to the sweep (with at most 25 % of matrices falling back); the
+final network is then fitted on all training matrices.
 
     python -m benchmark_spmv_using_csr_gb300.tuner_data.train [data_dir] [value type name ...]
 
@@ -22,8 +22,15 @@ import sys
 
 import numpy as np
 
-N_TRAIN = 2000
 EPOCHS, LR, WD = 300, 2e-3, 3e-4
+
+
+def split(done: int):
+    """(train, held-out) row indices of a timing table: matrices 0-1999 and 2200-2379 train,
+    2000-2199 and 2380-2399 (the last 20 of the large stratum) are held out."""
+    idx = np.arange(done)
+    held = ((idx >= 2000) & (idx < 2200)) | (idx >= 2380)
+    return idx[~held], idx[held]
 
 
 def _frac(ms, idx):
@@ -38,18 +45,23 @@ def train_one(data_dir: str, value_type: int) -> dict:
     done = int(d["done"])
     f, ms = d["features"][:done], d["ms"][:done].astype(np.float64)
     cands = [tuple(int(v) for v in c) for c in d["candidates"]]
-    ntr = min(N_TRAIN, done - max(done // 11, 1))
-    ftr, mtr, fte, mte = f[:ntr], ms[:ntr], f[ntr:], ms[ntr:]
-    nfit = int(0.85 * ntr)
+    tr, te = split(done)
+    ftr, mtr, fte, mte = f[tr], ms[tr], f[te], ms[te]
+    ntr = len(tr)
+    # the probe network's fit / calibration split: every 7th training matrix calibrates
+    cal = np.zeros(ntr, bool)
+    cal[::7] = True
     probe = mlp.LearnedTuner(n_out=ms.shape[1], seed=0, candidates=cands)
-    probe.fit(ftr[:nfit], mtr[:nfit], epochs=EPOCHS, batch=256, lr=LR, weight_decay=WD)
-    threshold = probe.calibrate_threshold(ftr[nfit:], mtr[nfit:], floor=0.95, max_fallback=0.25)
-    validation = probe.evaluate(ftr[nfit:], mtr[nfit:])
+    probe.fit(ftr[~cal], mtr[~cal], epochs=EPOCHS, batch=256, lr=LR, weight_decay=WD)
+    threshold = probe.calibrate_threshold(ftr[cal], mtr[cal], floor=0.95, max_fallback=0.25)
+    validation = probe.evaluate(ftr[cal], mtr[cal])
     tuner = mlp.LearnedTuner(n_out=ms.shape[1], seed=0, candidates=cands)
     hist = tuner.fit(ftr, mtr, epochs=EPOCHS, batch=256, lr=LR, weight_decay=WD)
     tuner.threshold = threshold
     ev_te = tuner.evaluate(fte, mte)
     ev_tr = tuner.evaluate(ftr, mtr)
+    large = te >= 2200
+    ev_large = tuner.evaluate(fte[large], mte[large]) if large.any() else None
     fixed = int(np.nan_to_num(mtr.min(1, keepdims=True) / mtr).mean(0).argmax())
     default = cands.index(tuple(sp.BhsparseSpmvCuda(value_type).get_config()))
     frac_fixed = _frac(mte, np.full(len(mte), fixed))
@@ -58,7 +70,7 @@ def train_one(data_dir: str, value_type: int) -> dict:
               "held_out_matrices": int(done - ntr),
               "final_train_loss": hist[-1], "first_train_loss": hist[0],
               "validation_of_threshold": validation,
-              "held_out": ev_te, "train": ev_tr,
+              "held_out": ev_te, "held_out_large_stratum": ev_large, "train": ev_tr,
               "best_fixed_schedule": list(cands[fixed]),
               "held_out_fixed_mean_frac_of_best": float(frac_fixed.mean()),
               "held_out_fixed_min_frac_of_best": float(frac_fixed.min()),

@@ -65,15 +65,17 @@ def test_committed_network_on_device_kernels(cuda_ok, name):
     time on average."""
     if not os.path.exists(_net_path(name)):
         pytest.skip("no trained network committed")
+    from benchmark_spmv_using_csr_gb300.tuner_data import train
     d = np.load(os.path.join(DATA, f"gb300_{name}_timings.npz"))
     done = int(d["done"])
     f, ms = d["features"][:done], d["ms"][:done]
+    _, te = train.split(done)
     tuner = mlp.LearnedTuner.load(_net_path(name))
-    ev = tuner.evaluate(f[2000:], ms[2000:])
+    ev = tuner.evaluate(f[te], ms[te])
     assert ev["mean_frac_of_best"] >= 0.95, ev
-    ref = mlp_oracle.forward(tuner.net.get_params(), f[2000:], tuner.net.mean, tuner.net.std,
+    ref = mlp_oracle.forward(tuner.net.get_params(), f[te], tuner.net.mean, tuner.net.std,
                              16, tuner.net.hidden, tuner.n_out)["p"]
-    np.testing.assert_allclose(tuner.net.forward(f[2000:]), ref, rtol=2e-4, atol=1e-6)
+    np.testing.assert_allclose(tuner.net.forward(f[te]), ref, rtol=2e-4, atol=1e-6)
 
 
 def _write_with_threshold(src, dst, threshold):

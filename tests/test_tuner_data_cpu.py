@@ -1,6 +1,6 @@
 """The committed learned tuners (one network per value type, trained on GB300 timing tables by
 the library's CUDA kernels), evaluated on the CPU with the numpy restatement of the network on
-the 200 held-out matrices of each committed timing table:
+the 220 held-out matrices of each committed timing table (tuner_data.train.split):
 
 * the picks, with the sweep standing in below the network's confidence threshold, reach >= 95 %
   of the autotuner-best time on average (the benchmark's target for the learned tuner);
@@ -16,6 +16,7 @@ import pytest
 
 from oracle import mlp_oracle
 from benchmark_spmv_using_csr_gb300 import mlp
+from benchmark_spmv_using_csr_gb300.tuner_data import train
 
 DATA = os.path.join(os.path.dirname(mlp.__file__), "tuner_data")
 NAMES = ["f64", "f32", "mixed_f32", "mixed_bf16"]
@@ -32,17 +33,17 @@ def test_committed_network_held_out(name):
     cands = [tuple(int(v) for v in c) for c in net["candidates"]]
     assert cands == [tuple(int(v) for v in c) for c in d["candidates"]]
     done = int(d["done"])
-    assert done == 2200
+    assert done == 2400
     f, ms = d["features"][:done], d["ms"][:done].astype(np.float64)
     p = mlp_oracle.forward(net["params"], f, net["mean"], net["std"], 16, net["hidden"],
                            net["n_out"])["p"]
     pick, conf = p.argmax(1), p.max(1)
     frac = ms.min(1) / ms[np.arange(done), pick]
-    te = slice(2000, 2200)
+    tr, te = train.split(done)
     fb = conf[te] < net["threshold"]
     with_fb = np.where(fb, 1.0, frac[te])
     assert with_fb.mean() >= 0.95
-    ftr = ms[:2000].min(1, keepdims=True) / ms[:2000]
+    ftr = ms[tr].min(1, keepdims=True) / ms[tr]
     fixed = int(ftr.mean(0).argmax())
     frac_fixed = ms[te].min(1) / ms[te][:, fixed]
     frac_default = ms[te].min(1) / ms[te][:, cands.index(DEFAULTS[name])]
