@@ -302,7 +302,7 @@ def run_ours(args) -> None:
     # the autotuner's full table on this matrix, for the report: the schedule itself is the one
     # prepare_mem chooses (the learned network, or the sweep below its confidence threshold),
     # as for any caller of the reference's API, unless --config sets one
-    tuning = autotune_workload(a, x)
+    tuning = autotune_workload(a, x) if args.tune_table else None
     h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
     if args.config is not None:
         assert h.set_config(*args.config) == 0, h.last_error
@@ -313,7 +313,9 @@ def run_ours(args) -> None:
     assert rc == 0, h.last_error
     t_prep = time.perf_counter() - t_prep
     seg, tpw, warps, stages = h.get_config()
-    tuning["prepare_mem_choice"] = schedule_choice(h, tuning)
+    choice = schedule_choice(h, tuning)
+    if tuning is not None:
+        tuning["prepare_mem_choice"] = choice
 
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
@@ -458,7 +460,7 @@ def run_ours(args) -> None:
                     "per_call": {"value": round(e2e_call_value, 2), "unit": UNIT,
                                  "path": "bhsp_set_x + bhsp_run_benchmark + bhsp_get_y per "
                                          "step, pinned host x / y"}},
-            "tuning": tuning,
+            "tuning": tuning if tuning is not None else {"prepare_mem_choice": choice},
             "gpu_launches": 2 * args.steps,
             "clocks": clocks,
             "prepare_mem_s": round(t_prep, 3),
@@ -836,6 +838,8 @@ def main() -> None:
                     metavar=("NNZ_PER_LANE", "TILES_PER_WORKER", "WARPS_PER_CTA", "STAGES"),
                     help="tile schedule (default: the autotuner's pick on this matrix)")
     ap.add_argument("--soak", type=float, default=1.5, help="seconds of untimed steps for clocks")
+    ap.add_argument("--no-tune-table", dest="tune_table", action="store_false",
+                    help="skip the autotuner's table of the headline matrix (it is only reported)")
     ap.add_argument("--cpu-baseline", type=float, default=10.0,
                     help="seconds of serial CPU baseline (0 = skip)")
     ap.add_argument("--no-forms", dest="forms", action="store_false")
