@@ -19,7 +19,7 @@ Metric: SpMV HBM GB/s on the algorithmic bytes B = nnz*(s_val+4) + (m+1)*4 + n*s
   K steps (copies of neighbouring steps overlap each SpMV); ``e2e.per_call`` is the
   reference's per-call sequence bhsp_set_x / bhsp_run_benchmark / bhsp_get_y.
 * ``sector_roofline`` (power-law matrix): L2 -> SM sectors per second against the random-gather
-  probe's rate, the unit that binds on that matrix.
+  probe's rate (307 G sectors/s), the unit that binds on that matrix.
 * ``roofline``: the tile kernel alone (launched on its own between CUDA events, L2 flushed
   before each) against the measured HBM copy bandwidth.
 * ``cpu_baseline``: the reference's serial CSR loop (spmv_cuda/main.cu:755-761, a port in
@@ -45,9 +45,11 @@ METRIC = "SpMV HBM GB/s (% of peak), mixed/batched vs plain FP64 at stated rel. 
 UNIT = "GB/s"
 FALLBACK_HBM_GBS = 6800.0
 FLUSH_BYTES = 256 << 20
-# fully random 8-byte gathers into a 33.5 MB L2-resident vector, all SMs, measured on GB300:
-# one 32-byte sector per gather
-SECTOR_PEAK_G = 289.0
+# 32-byte sectors per second the SMs take from L2 for random access, measured on GB300: 64 M fully
+# random 8-byte gathers into a 33.5 MB L2-resident vector, with their int32 column indices
+# streamed beside them (one sector per gather + 1/8 sector of index each): 273 G gathers/s, the
+# same through ld.global.nc, ld.global.cg and ld.global
+SECTOR_PEAK_G = 307.0
 
 
 def l2_sectors(a) -> int:
@@ -446,9 +448,10 @@ def run_ours(args) -> None:
                 "sectors_per_launch": l2_sectors(a),
                 "note": "32-byte sectors the SMs take from L2 per SpMV (one per random x gather, "
                         "plus val / col_idx / row_ptr at 32 bytes a sector) against the sector "
-                        "rate of a probe of fully random gathers into an L2-resident vector on "
-                        "GB300 (~1 sector per clock per SM); the binding unit on this matrix "
-                        "(ncu: l1tex__m_xbar2l1tex_read_sectors runs at this rate)"},
+                        "rate of a probe of fully random gathers, with streamed indices, into an "
+                        "L2-resident vector on GB300 (~1 sector per clock per SM, equal for the "
+                        "read-only, L2-only and plain load paths); the binding unit on this "
+                        "matrix"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic, "peak_kind": f"{peak_kind} (hbm_gbs copy, burst)",
