@@ -58,6 +58,29 @@ def autotune(value_type: int, row_ptr, col_idx, val, x, y, n: int | None = None,
     return ms, best.value
 
 
+def choose_schedule(value_type: int, row_ptr, col_idx, val, x, y, n: int | None = None,
+                    tuner: str | None = None, stream=None) -> dict:
+    """The schedule bhsp_choose_schedule picks for a device matrix (torch CUDA tensors): the
+    learned network's, or the sweep's below its confidence threshold.  tuner: None = the
+    library's network for value_type, "" = none, else a network file.  Returns {"config",
+    "source" (SCHEDULE_*), "confidence"}."""
+    L = lib()
+    c = [ctypes.c_int() for _ in range(4)]
+    src, conf = ctypes.c_int(), ctypes.c_float()
+    m = row_ptr.numel() - 1
+    n = x.numel() if n is None else n
+    rc = L.bhsp_choose_schedule(int(value_type), m, int(n), int(col_idx.numel()),
+                                row_ptr.data_ptr(), col_idx.data_ptr(), val.data_ptr(),
+                                x.data_ptr(), y.data_ptr(),
+                                None if tuner is None else tuner.encode(),
+                                *[ctypes.byref(v) for v in c], ctypes.byref(src),
+                                ctypes.byref(conf), ctypes.c_void_p(_stream_ptr(stream)))
+    if rc != 0:
+        raise RuntimeError(f"bhsp_choose_schedule failed with status {rc}")
+    return {"config": tuple(v.value for v in c), "source": src.value,
+            "confidence": float(conf.value)}
+
+
 def row_features(row_ptr, n: int, stream=None) -> np.ndarray:
     """The 16 row-length features, computed on the device from a torch CUDA row_ptr."""
     f = np.zeros(NUM_FEATURES, np.float32)

@@ -43,3 +43,45 @@ def test_autotune_picks_a_correct_schedule(cuda_ok, tmp_path):
     scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, x)
     err = oracle.componentwise_error(y.cpu().numpy(), oracle.csr_dot2(a.row_ptr, a.col, a.val, x), scale)
     assert err <= TOL_F64
+
+
+@pytest.mark.parametrize("vt", [sp.VALUE_F64, sp.VALUE_MIXED_BF16])
+def test_choose_schedule_on_device_buffers(cuda_ok, vt):
+    """bhsp_choose_schedule picks for caller-held device buffers what prepare_mem picks for the
+    same matrix through the handle, and a plan built with the pick computes the oracle's y."""
+    import torch
+    a = gen.stencil3d(60, 50, 40, seed=8)
+    x = gen.uniform(a.n, 9)
+    rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
+    v64 = torch.from_numpy(a.val).cuda()
+    if vt == sp.VALUE_F64:
+        val, xd = v64, torch.from_numpy(x).cuda()
+    else:
+        val, xd = v64.to(torch.bfloat16), torch.from_numpy(x).float().cuda()
+    y = torch.zeros(a.m, dtype=xd.dtype, device="cuda")
+    got = tune.choose_schedule(vt, rp, ci, val, xd, y)
+    assert got["config"] in tune.candidates() or got["source"] == sp.SCHEDULE_DEFAULT
+    h = sp.BhsparseSpmvCuda(vt)
+    yh = np.zeros(a.m)
+    assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x, yh) == 0, h.last_error
+    src, conf = h.schedule_source()
+    assert src == got["source"] and abs(conf - got["confidence"]) <= 1e-6
+    if src == sp.SCHEDULE_LEARNED:  # the sweep's timing may differ run to run; the network not
+        assert tuple(h.get_config()) == got["config"]
+    h.close()
+    none = tune.choose_schedule(vt, rp, ci, val, xd, y, tuner="")
+    assert none["source"] == sp.SCHEDULE_DEFAULT and none["confidence"] == 0.0
+    seg, tpw, warps, stages = got["config"]
+    p = sp.Plan(vt, a.m, a.n, rp, ci, seg=seg, tiles_per_worker=tpw, warps_per_cta=warps,
+                stages=stages)
+    y.fill_(float("nan"))
+    p.execute(val, xd, y)
+    p.check()
+    yy = y.double().cpu().numpy()
+    if vt == sp.VALUE_F64:
+        scale = oracle.csr_absrow(a.row_ptr, a.col, a.val, x)
+        assert oracle.componentwise_error(yy, oracle.csr_dot2(a.row_ptr, a.col, a.val, x),
+                                          scale) <= TOL_F64
+    else:
+        assert np.all(np.isfinite(yy))
+    p.close()
