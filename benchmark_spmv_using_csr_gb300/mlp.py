@@ -15,6 +15,7 @@ from . import tune
 from ._lib import lib
 
 HIDDEN = 64
+RISK_HIDDEN = 32
 
 
 def soft_targets(ms: np.ndarray, temperature: float = 0.05) -> np.ndarray:
@@ -143,37 +144,47 @@ class LearnedTuner:
             raise ValueError("one network output per candidate schedule")
         self.net = MLP(tune.NUM_FEATURES, hidden, self.n_out, seed=seed)
         self.threshold = 0.0
+        # the optional risk network and its threshold (fallback where its P(slow pick) exceeds it)
+        self.risk = None
+        self.risk_threshold = 1.0
 
     def fit(self, feats: np.ndarray, ms: np.ndarray, epochs: int = 400, batch: int = 256,
             lr: float = 3e-3, weight_decay: float = 1e-4, temperature: float = 0.05,
             seed: int = 0) -> list:
         """Train on (features, timing table) pairs with the device kernels; returns the
         per-epoch mean loss."""
-        import torch
-        feats = np.asarray(feats, np.float32)
-        mean, std = feats.mean(0), feats.std(0)
-        std[std < 1e-6] = 1.0
-        self.net.set_normalization(mean, std)
-        targets = soft_targets(ms, temperature)
-        f_dev, t_dev = self.net._dev(feats), self.net._dev(targets)
-        rng = np.random.default_rng(seed)
-        hist = []
-        n = feats.shape[0]
-        for ep in range(epochs):
-            perm = torch.from_numpy(rng.permutation(n)).cuda()
-            step_lr = lr * 0.5 * (1 + np.cos(np.pi * ep / epochs))  # cosine decay
-            losses = []
-            for s in range(0, n, batch):
-                idx = perm[s:s + batch]
-                losses.append(self.net.train_step(f_dev[idx].contiguous(), t_dev[idx].contiguous(),
-                                                  step_lr, weight_decay))
-            hist.append(float(np.mean(losses)))
-        return hist
+        return train_net(self.net, feats, soft_targets(ms, temperature), epochs, batch, lr,
+                         weight_decay, seed)
+
+    def fit_risk(self, feats: np.ndarray, probs: np.ndarray, bad: np.ndarray,
+                 hidden: int = RISK_HIDDEN, epochs: int = 300, batch: int = 256,
+                 lr: float = 2e-3, weight_decay: float = 3e-4, seed: int = 1) -> list:
+        """Train the risk network: from the features and the schedule network's output
+        distribution (its picks made on matrices it was not fitted on) to whether the pick is
+        slow (`bad`, e.g. below 95 % of the best time).  The sweep is the fallback where the
+        risk is above risk_threshold."""
+        x = risk_inputs(feats, probs)
+        self.risk = MLP(x.shape[1], hidden, 2, seed=seed)
+        b = np.asarray(bad, np.float32)
+        return train_net(self.risk, x, np.stack([1.0 - b, b], 1), epochs, batch, lr,
+                         weight_decay, seed)
 
     def predict(self, feats: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         """(picked candidate index, confidence = its probability) per row of features."""
         p = self.net.forward(np.atleast_2d(feats))
         return p.argmax(1), p.max(1)
+
+    def fallback(self, feats: np.ndarray):
+        """(picks, whether each goes to the sweep, confidence, risk): the sweep decides where
+        the risk network's P(slow pick) exceeds risk_threshold, or, without a risk network,
+        where the confidence is below the threshold."""
+        feats = np.atleast_2d(feats)
+        p = self.net.forward(feats)
+        pick, conf = p.argmax(1), p.max(1)
+        if self.risk is not None:
+            r = self.risk.forward(risk_inputs(feats, p))[:, 1]
+            return pick, r > self.risk_threshold, conf, r
+        return pick, conf < self.threshold, conf, np.zeros_like(conf)
 
     def calibrate_threshold(self, feats, ms, floor: float = 0.95, max_fallback: float = 0.25) -> float:
         """Confidence threshold from matrices the network was not fitted on: the smallest one
@@ -195,8 +206,7 @@ class LearnedTuner:
     def evaluate(self, feats, ms) -> dict:
         """Fraction of the autotuner's best time per matrix (best_ms / picked_ms), with the
         sweep standing in below the confidence threshold."""
-        pick, conf = self.predict(feats)
-        fb = conf < self.threshold
+        pick, fb, _, _ = self.fallback(feats)
         frac = ms.min(1) / ms[np.arange(len(pick)), pick]
         frac_with_fb = np.where(fb, 1.0, frac)
         return {"mean_frac_of_best": float(frac_with_fb.mean()),
@@ -205,7 +215,8 @@ class LearnedTuner:
                 "min_frac_without_fallback": float(frac.min()),
                 "picks_below_95pct_kept": int(np.sum((frac < 0.95) & ~fb)),
                 "picks_below_95pct_without_fallback": int(np.sum(frac < 0.95)),
-                "fallback_rate": float(fb.mean()), "threshold": self.threshold}
+                "fallback_rate": float(fb.mean()), "threshold": self.threshold,
+                "risk_threshold": self.risk_threshold if self.risk is not None else None}
 
     def choose(self, value_type: int, row_ptr, col_idx, val, x, y, n: int | None = None) -> dict:
         """Pick a schedule for a device matrix: the network if confident, else the sweep."""
@@ -213,8 +224,8 @@ class LearnedTuner:
             raise ValueError("this network's outputs are not tied to candidate schedules")
         n = x.numel() if n is None else n
         f = tune.row_features(row_ptr, n)
-        pick, conf = self.predict(f)
-        if conf[0] >= self.threshold:
+        pick, fb, conf, _ = self.fallback(f)
+        if not fb[0]:
             return {"index": int(pick[0]), "confidence": float(conf[0]), "fallback": False,
                     "config": self.candidates[int(pick[0])]}
         ms, best = tune.autotune(value_type, row_ptr, col_idx, val, x, y, n=n)
@@ -226,8 +237,13 @@ class LearnedTuner:
         sizes, threshold, input standardisation, candidate schedules, parameters."""
         if self.candidates is None:
             raise ValueError("only a network tied to candidate schedules can be saved")
+        risk = None
+        if self.risk is not None:
+            risk = {"hidden": self.risk.hidden, "threshold": self.risk_threshold,
+                    "mean": self.risk.mean, "std": self.risk.std, "params": self.risk.get_params()}
         write_network(path, value_type, self.net.hidden, self.threshold, self.net.mean,
-                      self.net.std, np.array(self.candidates, np.int32), self.net.get_params())
+                      self.net.std, np.array(self.candidates, np.int32), self.net.get_params(),
+                      risk)
 
     @classmethod
     def load(cls, path: str) -> "LearnedTuner":
@@ -237,15 +253,57 @@ class LearnedTuner:
         t.net.set_normalization(d["mean"], d["std"])
         t.threshold = d["threshold"]
         t.value_type = d["value_type"]
+        r = d.get("risk")
+        if r is not None:
+            t.risk = MLP(r["n_in"], r["hidden"], 2)
+            t.risk.set_params(r["params"])
+            t.risk.set_normalization(r["mean"], r["std"])
+            t.risk_threshold = r["threshold"]
         return t
 
 
 MAGIC = b"BHSPTUN1"
+RISK_MAGIC = b"BHSPRSK1"
+
+
+def risk_inputs(feats: np.ndarray, probs: np.ndarray) -> np.ndarray:
+    """The risk network's inputs: the 16 row features, then the schedule network's largest and
+    second-largest probability and the entropy of its distribution."""
+    f = np.atleast_2d(np.asarray(feats, np.float32))
+    p = np.atleast_2d(np.asarray(probs, np.float64))
+    top = np.sort(p, 1)
+    ent = -(p * np.log(np.maximum(p, 1e-30))).sum(1)
+    return np.concatenate([f, top[:, -1:], top[:, -2:-1], ent[:, None]], 1).astype(np.float32)
+
+
+def train_net(net: "MLP", x: np.ndarray, targets: np.ndarray, epochs: int, batch: int,
+              lr: float, weight_decay: float, seed: int) -> list:
+    """Mini-batch Adam with cosine decay over (inputs, target distributions), all in the device
+    kernels; standardises the inputs first.  Returns the per-epoch mean loss."""
+    import torch
+    x = np.asarray(x, np.float32)
+    mean, std = x.mean(0), x.std(0)
+    std[std < 1e-6] = 1.0
+    net.set_normalization(mean, std)
+    f_dev, t_dev = net._dev(x), net._dev(np.asarray(targets, np.float32))
+    rng = np.random.default_rng(seed)
+    hist = []
+    n = x.shape[0]
+    for ep in range(epochs):
+        perm = torch.from_numpy(rng.permutation(n)).cuda()
+        step_lr = lr * 0.5 * (1 + np.cos(np.pi * ep / epochs))
+        losses = []
+        for s in range(0, n, batch):
+            idx = perm[s:s + batch]
+            losses.append(net.train_step(f_dev[idx].contiguous(), t_dev[idx].contiguous(),
+                                         step_lr, weight_decay))
+        hist.append(float(np.mean(losses)))
+    return hist
 
 
 def write_network(path: str, value_type: int, hidden: int, threshold: float, mean, std,
-                  candidates: np.ndarray, params: np.ndarray) -> None:
-    """The little-endian network file of csrc/learned.cu."""
+                  candidates: np.ndarray, params: np.ndarray, risk: dict | None = None) -> None:
+    """The little-endian network file of csrc/learned.cu, with the optional risk section."""
     cands = np.ascontiguousarray(candidates, "<i4").reshape(-1, 4)
     mean = np.ascontiguousarray(mean, "<f4")
     std = np.ascontiguousarray(std, "<f4")
@@ -259,6 +317,17 @@ def write_network(path: str, value_type: int, hidden: int, threshold: float, mea
         f.write(cands.tobytes())
         f.write(np.array([params.size], "<i4").tobytes())
         f.write(params.tobytes())
+        if risk is not None:
+            rm = np.ascontiguousarray(risk["mean"], "<f4")
+            rs = np.ascontiguousarray(risk["std"], "<f4")
+            rp = np.ascontiguousarray(risk["params"], "<f4")
+            f.write(RISK_MAGIC)
+            f.write(np.array([rm.size, risk["hidden"], 2], "<i4").tobytes())
+            f.write(np.array([risk["threshold"]], "<f4").tobytes())
+            f.write(rm.tobytes())
+            f.write(rs.tobytes())
+            f.write(np.array([rp.size], "<i4").tobytes())
+            f.write(rp.tobytes())
 
 
 def read_network(path: str) -> dict:
@@ -278,8 +347,28 @@ def read_network(path: str) -> dict:
     npar = int(np.frombuffer(raw, "<i4", 1, o)[0])
     o += 4
     params = np.frombuffer(raw, "<f4", npar, o).copy()
-    if o + 4 * npar != len(raw):
+    o += 4 * npar
+    risk = None
+    if o < len(raw):
+        if raw[o:o + 8] != RISK_MAGIC:
+            raise ValueError(f"{path}: unknown section after the parameters")
+        o += 8
+        r_in, r_hidden, r_out = (int(v) for v in np.frombuffer(raw, "<i4", 3, o))
+        o += 12
+        r_th = float(np.frombuffer(raw, "<f4", 1, o)[0])
+        o += 4
+        r_mean = np.frombuffer(raw, "<f4", r_in, o).copy()
+        o += 4 * r_in
+        r_std = np.frombuffer(raw, "<f4", r_in, o).copy()
+        o += 4 * r_in
+        r_np = int(np.frombuffer(raw, "<i4", 1, o)[0])
+        o += 4
+        r_params = np.frombuffer(raw, "<f4", r_np, o).copy()
+        o += 4 * r_np
+        risk = {"n_in": r_in, "hidden": r_hidden, "n_out": r_out, "threshold": r_th,
+                "mean": r_mean, "std": r_std, "params": r_params}
+    if o != len(raw):
         raise ValueError(f"{path}: trailing or missing bytes")
     return {"value_type": vt, "n_in": n_in, "hidden": hidden, "n_out": n_out,
             "threshold": threshold, "mean": mean, "std": std, "candidates": cands,
-            "params": params}
+            "params": params, "risk": risk}

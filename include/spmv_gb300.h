@@ -253,10 +253,13 @@ int bhsp_autotune(int value_type, int m, int n, int nnz, const int* d_row_ptr,
 #define BHSP_SCHEDULE_LEARNED 2 /* the learned network's pick */
 #define BHSP_SCHEDULE_SWEEP 3   /* the full autotune sweep: the network was below its threshold */
 /* The schedule for a matrix held on the device: the 16 row features (bhsp_row_features) go
- * through the learned network's forward kernels; its most probable candidate is taken when that
- * probability reaches the network's calibrated confidence threshold, else the full autotune
- * sweep (bhsp_autotune, 1 warm-up and the median of 3 flushed-L2 runs per candidate, writing
- * d_y) decides.  tuner_path: NULL = the library's network for value_type, the file
+ * through the learned network's forward kernels, and its most probable candidate is taken
+ * unless a second, small risk network (the features and the first network's top two
+ * probabilities and entropy in, the probability that the pick is below 95 % of the best time
+ * out) rates the pick as likely slow, or the pick's probability is below the file's confidence
+ * threshold; then the full autotune sweep (bhsp_autotune, 1 warm-up and the median of 3
+ * flushed-L2 runs per candidate, writing d_y) decides.  *confidence is the first network's
+ * probability of its pick.  tuner_path: NULL = the library's network for value_type, the file
  * tuner_data/gb300_<f64|f32|mixed_f32|mixed_bf16>_tuner.bin next to the library (or in the
  * directory named by the BHSP_TUNER_DIR environment variable); with no such file the fixed
  * default is returned (*source = BHSP_SCHEDULE_DEFAULT).  "" = no network (the fixed default).

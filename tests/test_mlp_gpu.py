@@ -78,10 +78,15 @@ def test_committed_network_on_device_kernels(cuda_ok, name):
     np.testing.assert_allclose(tuner.net.forward(f[te]), ref, rtol=2e-4, atol=1e-6)
 
 
-def _write_with_threshold(src, dst, threshold):
+def _write_with_threshold(src, dst, threshold, risk_threshold=None):
+    """A copy of a network file with its confidence threshold (and its risk network's
+    threshold, when given) replaced."""
     d = mlp.read_network(src)
+    risk = d["risk"]
+    if risk is not None and risk_threshold is not None:
+        risk = dict(risk, threshold=risk_threshold)
     mlp.write_network(dst, d["value_type"], d["hidden"], threshold, d["mean"], d["std"],
-                      d["candidates"], d["params"])
+                      d["candidates"], d["params"], risk)
     return d
 
 
@@ -101,8 +106,8 @@ def _prepare(vt, a, x, tuner=None):
 def test_prepare_mem_takes_the_networks_pick(cuda_ok, tmp_path, vt):
     """Without bhsp_set_config, prepare_mem runs the learned network on the matrix's features
     (forward kernel on the device) and takes its most probable schedule when the network is
-    confident: with the threshold set to 0 the schedule equals the argmax of the numpy
-    restatement of the network on the same features."""
+    confident: with both thresholds opened (confidence 0, risk 1) the schedule equals the argmax
+    of the numpy restatement of the network on the same features."""
     import torch
 
     import benchmark_spmv_using_csr_gb300 as sp
@@ -111,7 +116,7 @@ def test_prepare_mem_takes_the_networks_pick(cuda_ok, tmp_path, vt):
     if not os.path.exists(_net_path(name)):
         pytest.skip("no trained network committed")
     path = str(tmp_path / "net.bin")
-    d = _write_with_threshold(_net_path(name), path, 0.0)
+    d = _write_with_threshold(_net_path(name), path, 0.0, risk_threshold=1.0)
     for a in (gen.powerlaw(200_000, seed=3), gen.stencil3d(50, 40, 30, seed=4)):
         x = gen.uniform(a.n, 5)
         h, y = _prepare(vt, a, x, path)
@@ -178,3 +183,42 @@ def test_schedule_sources(cuda_ok):
     assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x, y) == \
         sp.BHSPARSE_INVALID_ARGUMENT
     h.close()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_risk_network_decides_the_fallback(cuda_ok, tmp_path, name):
+    """The C path runs the file's risk network on the features and the schedule network's
+    output: with the risk threshold at 0 (every pick rated slow) the matrix goes to the sweep,
+    with it at 1 it takes the network's pick; the numpy restatement of both networks gives the
+    risk the device computes."""
+    import torch
+
+    import benchmark_spmv_using_csr_gb300 as sp
+    from benchmark_spmv_using_csr_gb300 import gen, tune
+    if not os.path.exists(_net_path(name)):
+        pytest.skip("no trained network committed")
+    d = mlp.read_network(_net_path(name))
+    if d["risk"] is None:
+        pytest.skip("network file without a risk network")
+    vt = {"f64": 0, "f32": 1, "mixed_f32": 2, "mixed_bf16": 3}[name]
+    a = gen.powerlaw(150_000, seed=12)
+    x = gen.uniform(a.n, 13)
+    sweep, learned = str(tmp_path / "sweep.bin"), str(tmp_path / "learned.bin")
+    _write_with_threshold(_net_path(name), sweep, 0.0, risk_threshold=0.0)
+    _write_with_threshold(_net_path(name), learned, 0.0, risk_threshold=1.0)
+    h, _ = _prepare(vt, a, x, sweep)
+    assert h.schedule_source()[0] == sp.SCHEDULE_SWEEP
+    h.close()
+    h, _ = _prepare(vt, a, x, learned)
+    assert h.schedule_source()[0] == sp.SCHEDULE_LEARNED
+    h.close()
+    f = tune.row_features(torch.from_numpy(a.row_ptr).cuda(), a.n)
+    p = mlp_oracle.forward(d["params"], f[None], d["mean"], d["std"], 16, d["hidden"],
+                           d["n_out"])["p"]
+    r = d["risk"]
+    risk = mlp_oracle.forward(r["params"], mlp.risk_inputs(f[None], p), r["mean"], r["std"],
+                              r["n_in"], r["hidden"], 2)["p"][0, 1]
+    tuner = mlp.LearnedTuner.load(_net_path(name))
+    _, fb, _, r_dev = tuner.fallback(f[None])
+    assert abs(float(r_dev[0]) - risk) <= 1e-4
+    assert bool(fb[0]) == (risk > r["threshold"])

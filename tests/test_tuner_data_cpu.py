@@ -41,6 +41,11 @@ def test_committed_network_held_out(name):
     frac = ms.min(1) / ms[np.arange(done), pick]
     tr, te = train.split(done)
     fb = conf[te] < net["threshold"]
+    r = net["risk"]
+    if r is not None:  # the risk network decides the fallback
+        risk = mlp_oracle.forward(r["params"], mlp.risk_inputs(f[te], p[te]), r["mean"],
+                                  r["std"], r["n_in"], r["hidden"], 2)["p"][:, 1]
+        fb = fb | (risk > r["threshold"])
     with_fb = np.where(fb, 1.0, frac[te])
     assert with_fb.mean() >= 0.95
     ftr = ms[tr].min(1, keepdims=True) / ms[tr]
