@@ -19,7 +19,7 @@ Metric: SpMV HBM GB/s on the algorithmic bytes B = nnz*(s_val+4) + (m+1)*4 + n*s
   K steps (copies of neighbouring steps overlap each SpMV); ``e2e.per_call`` is the
   reference's per-call sequence bhsp_set_x / bhsp_run_benchmark / bhsp_get_y.
 * ``sector_roofline`` (power-law matrix): L2 -> SM sectors per second against the random-gather
-  probe's rate (307 G sectors/s), the unit that binds on that matrix.
+  probe's rate (323 G sectors/s), the unit that binds on that matrix.
 * ``roofline``: the tile kernel alone (launched on its own between CUDA events, L2 flushed
   before each) against the measured HBM copy bandwidth.
 * ``cpu_baseline``: the reference's serial CSR loop (spmv_cuda/main.cu:755-761, a port in
@@ -45,11 +45,12 @@ METRIC = "SpMV HBM GB/s (% of peak), mixed/batched vs plain FP64 at stated rel. 
 UNIT = "GB/s"
 FALLBACK_HBM_GBS = 6800.0
 FLUSH_BYTES = 256 << 20
-# 32-byte sectors per second the SMs take from L2 for random access, measured on GB300: 64 M fully
-# random 8-byte gathers into a 33.5 MB L2-resident vector, with their int32 column indices
-# streamed beside them (one sector per gather + 1/8 sector of index each): 273 G gathers/s, the
-# same through ld.global.nc, ld.global.cg and ld.global
-SECTOR_PEAK_G = 307.0
+# 32-byte sectors per second the SMs take from L2 for random access, measured on GB300 by
+# `python -m benchmark_spmv_using_csr_gb300.probes`: 64 M fully random 8-byte gathers into a
+# 33.5 MB L2-resident vector, with their int32 column indices streamed beside them (one sector
+# per gather + 1/8 sector of index each): 287 G gathers/s, the same through ld.global.nc,
+# ld.global.cg and ld.global
+SECTOR_PEAK_G = 323.0
 
 
 def l2_sectors(a) -> int:

@@ -568,17 +568,32 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     if (!rec_written && lane == 0) a.rec_row[worker] = -1;
 }
 
-// Resident warps per SM asked of the register allocator: 24 for S = 8 (80 registers), 16 for
-// S = 16 and S = 32 (128 registers).  Left alone, the FP64 S = 32 kernel takes 136 registers
-// and 12 warps; at 128 it does not spill and runs 13 % faster on the 27-point stencil.
-template <int S, int WARPS>
-struct MinBlocks {
-    static constexpr int value = S == 8 ? 24 / WARPS : 16 / WARPS;
-};
+// Resident warps per SM asked of the register allocator (the launch bound is that many warps
+// divided by the warps of a CTA), measured per arithmetic policy on the 27-point stencil and the
+// power-law matrix at 16, 20 and 24 warps (4-warp CTAs):
+//  * S = 8: 24 (80 registers) for every policy;
+//  * plain FP64 at S = 16 and 32: 16 (128 registers).  Left alone the S = 32 kernel takes 136
+//    registers and 12 warps; at 128 it does not spill and runs 13 % faster on the stencil, while
+//    20 or 24 warps spill and run 1.5-2.4x slower;
+//  * plain FP32: 24 at S = 16 (-5.4 % on the stencil, -1.5 % on the power-law matrix against
+//    16) and 20 at S = 32 (-5.2 % on the stencil);
+//  * the mixed forms: 20 (mixed FP32 -3.8 % at S = 32 and -10.5 % at S = 16 on the stencil,
+//    -2.1 % at S = 16 on the power-law matrix; BF16 values -12 % at S = 16).
+template <class P, int S>
+constexpr int resident_warps() {
+    if constexpr (S == 8)
+        return 24;
+    else if constexpr (std::is_same<typename P::VC, double>::value)
+        return 16;
+    else if constexpr (std::is_same<typename P::Acc, float>::value)
+        return S == 16 ? 24 : 20;
+    else
+        return 20;
+}
 
 // One warp = one worker, worker = global warp index (static schedule).
 template <class P, int S, int WARPS, bool OH, bool XL2>
-__global__ void __launch_bounds__(WARPS * 32, (MinBlocks<S, WARPS>::value))
+__global__ void __launch_bounds__(WARPS * 32, (resident_warps<P, S>() / WARPS))
     k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
     // Plain FP64 with the one-head form (long rows) keeps two slot -> row maps per warp where
     // they fit in 40 KB (all but S = 32 at 8 warps), so that the next tile's map is built half-
