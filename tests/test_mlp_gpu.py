@@ -222,3 +222,26 @@ def test_risk_network_decides_the_fallback(cuda_ok, tmp_path, name):
     _, fb, _, r_dev = tuner.fallback(f[None])
     assert abs(float(r_dev[0]) - risk) <= 1e-4
     assert bool(fb[0]) == (risk > r["threshold"])
+
+
+def test_malformed_or_mismatched_network_files_are_refused(cuda_ok, tmp_path):
+    """prepare_mem refuses a network file that is truncated, has trailing bytes, or was trained
+    for another value type, instead of reading a schedule out of it."""
+    import benchmark_spmv_using_csr_gb300 as sp
+    from benchmark_spmv_using_csr_gb300 import gen
+    if not os.path.exists(_net_path("f64")):
+        pytest.skip("no trained network committed")
+    raw = open(_net_path("f64"), "rb").read()
+    a = gen.stencil2d(40, 30)
+    x = gen.uniform(a.n, 2)
+    bad = {"truncated.bin": raw[:-7], "trailing.bin": raw + b"junk", "empty.bin": b"",
+           "f32.bin": open(_net_path("f32"), "rb").read()}
+    for name, data in bad.items():
+        path = tmp_path / name
+        path.write_bytes(data)
+        h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+        assert h.set_tuner(str(path)) == 0
+        y = np.zeros(a.m)
+        assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x, y) == \
+            sp.BHSPARSE_INVALID_ARGUMENT, name
+        h.close()
