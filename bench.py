@@ -411,6 +411,26 @@ def run_ours(args) -> None:
     e2e_call_s = max_over_ranks(time.perf_counter() - t0, dist)
     barrier()
     e2e_call_value = whole_job_gbs(world, B, args.steps, e2e_call_s)
+    # the same per-call sequence on pageable host arrays, as the reference's driver allocates them
+    # (malloc); a second handle at the same schedule
+    x_pg, y_pg = x.copy(), np.zeros(a.m)
+    h2 = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+    assert h2.set_config(seg, tpw, warps, stages) == 0 and h2.set_device(local) == 0
+    assert h2.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, a.val, x_pg, y_pg) == 0, h2.last_error
+    for _ in range(3):
+        assert h2.set_x(x_pg) == 0 and h2.run_benchmark() == 0 and h2.get_y() == 0
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        assert h2.set_x(x_pg) == 0, h2.last_error
+        assert h2.run_benchmark() == 0, h2.last_error
+        assert h2.get_y() == 0, h2.last_error
+    e2e_pg_s = max_over_ranks(time.perf_counter() - t0, dist)
+    barrier()
+    e2e_pg_value = whole_job_gbs(world, B, args.steps, e2e_pg_s)
+    assert np.array_equal(y_pg, y_np)
+    h2.free_mem()
+    h2.close()
 
     # correctness of the benchmarked y against the FP64 compensated oracle
     ystar = oracle.csr_dot2(a.row_ptr, a.col, a.val, x)
@@ -463,7 +483,12 @@ def run_ours(args) -> None:
                             "x_{i+1} and download of y_{i-1} overlap SpMV i)",
                     "per_call": {"value": round(e2e_call_value, 2), "unit": UNIT,
                                  "path": "bhsp_set_x + bhsp_run_benchmark + bhsp_get_y per "
-                                         "step, pinned host x / y"}},
+                                         "step, pinned host x / y"},
+                    "per_call_pageable": {"value": round(e2e_pg_value, 2), "unit": UNIT,
+                                          "path": "the same per-call sequence on pageable "
+                                                  "(malloc'd) host x / y, copied by a kernel "
+                                                  "where the device reads and writes pageable "
+                                                  "memory"}},
             "tuning": tuning if tuning is not None else {"prepare_mem_choice": choice},
             "gpu_launches": 2 * args.steps,
             "clocks": clocks,

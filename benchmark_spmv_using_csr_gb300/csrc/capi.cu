@@ -564,11 +564,10 @@ static void handle_release(bhsp_spmv* h) {
 static int upload_values(bhsp_spmv* h, void* dst, const void* src, size_t count, bool is_matrix) {
     if (count == 0) return BHSPARSE_SUCCESS;
     if (h->vt == BHSP_VALUE_F64 || h->vt == BHSP_VALUE_F32) {
-        H_CUDA(h, cudaMemcpyAsync(dst, src, count * host_bytes(h->vt), cudaMemcpyHostToDevice,
-                                  h->stream));
+        H_CUDA(h, host_copy(dst, src, count * host_bytes(h->vt), false, h->stream));
         return BHSPARSE_SUCCESS;
     }
-    H_CUDA(h, cudaMemcpyAsync(h->d_stage, src, count * 8, cudaMemcpyHostToDevice, h->stream));
+    H_CUDA(h, host_copy(h->d_stage, src, count * 8, false, h->stream));
     const bool to_bf16 = is_matrix && h->vt == BHSP_VALUE_MIXED_BF16;
     H_CUDA(h, launch_convert_from_f64(h->d_stage, dst, count, to_bf16, h->stream));
     return BHSPARSE_SUCCESS;
@@ -603,11 +602,8 @@ extern "C" int bhsp_prepare_mem(bhsp_spmv* h, int m, int n, int nnz, const int* 
         if ((size_t)nnz > big) big = nnz;
         H_CUDA(h, cudaMalloc(&h->d_stage, 8 * (big > 0 ? big : 1)));
     }
-    H_CUDA(h, cudaMemcpyAsync(h->d_row_ptr, row_ptr, sizeof(int) * ((size_t)m + 1),
-                              cudaMemcpyHostToDevice, h->stream));
-    if (nnz > 0)
-        H_CUDA(h, cudaMemcpyAsync(h->d_col, col_idx, sizeof(int) * (size_t)nnz,
-                                  cudaMemcpyHostToDevice, h->stream));
+    H_CUDA(h, host_copy(h->d_row_ptr, row_ptr, sizeof(int) * ((size_t)m + 1), false, h->stream));
+    if (nnz > 0) H_CUDA(h, host_copy(h->d_col, col_idx, sizeof(int) * (size_t)nnz, false, h->stream));
     rc = upload_values(h, h->d_val, val, (size_t)nnz, true);
     if (rc) return rc;
     rc = upload_values(h, h->d_x, x, (size_t)n, false);
@@ -662,7 +658,11 @@ extern "C" int bhsp_set_x(bhsp_spmv* h, const void* x) {
     if (!h) return BHSPARSE_INVALID_ARGUMENT;
     if (!h->prepared) return h_fail(h, BHSPARSE_NOT_PREPARED, "set_x before prepare_mem");
     if (h->n > 0 && !x) return h_fail(h, BHSPARSE_INVALID_ARGUMENT, "null x");
-    return upload_values(h, h->d_x, x, (size_t)h->n, false);
+    const int rc = upload_values(h, h->d_x, x, (size_t)h->n, false);
+    if (rc) return rc;
+    // the caller may reuse its buffer as soon as this returns
+    H_CUDA(h, cudaStreamSynchronize(h->stream));
+    return BHSPARSE_SUCCESS;
 }
 
 extern "C" int bhsp_run_async(bhsp_spmv* h, void* stream) {
@@ -701,13 +701,11 @@ extern "C" int bhsp_get_y(bhsp_spmv* h) {
     if (!h->prepared) return h_fail(h, BHSPARSE_NOT_PREPARED, "get_y before prepare_mem");
     if (h->m == 0) return BHSPARSE_SUCCESS;
     if (h->vt == BHSP_VALUE_F64 || h->vt == BHSP_VALUE_F32) {
-        H_CUDA(h, cudaMemcpyAsync(h->h_y, h->d_y, (size_t)h->m * vec_bytes(h->vt),
-                                  cudaMemcpyDeviceToHost, h->stream));
+        H_CUDA(h, host_copy(h->h_y, h->d_y, (size_t)h->m * vec_bytes(h->vt), true, h->stream));
     } else {
         H_CUDA(h, launch_convert_to_f64(static_cast<const float*>(h->d_y), h->d_stage, (size_t)h->m,
                                         h->stream));
-        H_CUDA(h, cudaMemcpyAsync(h->h_y, h->d_stage, (size_t)h->m * 8, cudaMemcpyDeviceToHost,
-                                  h->stream));
+        H_CUDA(h, host_copy(h->h_y, h->d_stage, (size_t)h->m * 8, true, h->stream));
     }
     H_CUDA(h, cudaStreamSynchronize(h->stream));
     return BHSPARSE_SUCCESS;

@@ -1,0 +1,74 @@
+// hostcopy.cu -- copies between device memory and pageable host memory by a kernel.
+//
+// On a Grace host the GPU reads and writes the CPU's pageable memory coherently through the
+// host's page tables (cudaDevAttrPageableMemoryAccess and
+// cudaDevAttrPageableMemoryAccessUsesHostPageTables both 1).  A copy kernel over such memory
+// moves 33.5 MB at 196 GB/s where cudaMemcpy from the same pageable buffer, staged through pinned
+// bounce buffers by the driver, reaches 160 GB/s (pinned memory: about 205 GB/s either way).  The
+// handle API uses it for the caller's arrays when they are pageable: the reference's callers pass
+// plain malloc'd arrays (spmv_cuda/main.cu:745-746).
+#include <atomic>
+
+#include "internal.h"
+
+namespace spmv {
+namespace {
+
+__global__ void k_copy16(const int4* __restrict__ src, int4* __restrict__ dst, long long n16,
+                         const unsigned char* __restrict__ src_tail,
+                         unsigned char* __restrict__ dst_tail, int tail) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (long long i = tid; i < n16; i += stride) dst[i] = src[i];
+    if (tid < tail) dst_tail[tid] = src_tail[tid];
+}
+
+}  // namespace
+
+bool host_direct_access() {
+    static std::atomic<int> cache[64];  // 0: not looked up, 1: no, 2: yes
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return false;
+    if (dev < 64) {
+        const int c = cache[dev].load(std::memory_order_relaxed);
+        if (c) return c == 2;
+    }
+    int pageable = 0, host_tables = 0;
+    const bool ok =
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                               dev) == cudaSuccess &&
+        pageable == 1 && host_tables == 1;
+    if (dev < 64) cache[dev].store(ok ? 2 : 1, std::memory_order_relaxed);
+    return ok;
+}
+
+bool is_pageable_host(const void* p) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the query's error
+        return false;
+    }
+    return attr.type == cudaMemoryTypeUnregistered;
+}
+
+cudaError_t host_copy(void* dst, const void* src, size_t bytes, bool device_to_host,
+                      cudaStream_t st) {
+    if (bytes == 0) return cudaSuccess;
+    const void* host = device_to_host ? dst : src;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) &
+                          15u) == 0u;
+    if (!aligned || !host_direct_access() || !is_pageable_host(host))
+        return cudaMemcpyAsync(dst, src, bytes,
+                               device_to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice,
+                               st);
+    const long long n16 = (long long)(bytes / 16);
+    const int tail = (int)(bytes % 16);
+    const int grid = grid_for(n16 > tail ? n16 : tail, 512, 4);
+    k_copy16<<<grid, 512, 0, st>>>(static_cast<const int4*>(src), static_cast<int4*>(dst), n16,
+                                   static_cast<const unsigned char*>(src) + 16 * n16,
+                                   static_cast<unsigned char*>(dst) + 16 * n16, tail);
+    return cudaGetLastError();
+}
+
+}  // namespace spmv

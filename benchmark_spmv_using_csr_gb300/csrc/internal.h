@@ -13,6 +13,15 @@ int device_sm_count();
 // min(ceil(work / threads), cap_per_sm * SMs), at least 1: the grid of a grid-stride launch
 int grid_for(long long work, int threads, int cap_per_sm);
 
+// hostcopy.cu: host <-> device copies for the handle API.  The device reads / writes pageable
+// host memory coherently where it has pageable memory access through the host's page tables
+// (Grace); host_copy then uses a copy kernel for pageable, 16-byte-aligned host buffers and
+// cudaMemcpyAsync otherwise.
+bool host_direct_access();
+bool is_pageable_host(const void* p);
+cudaError_t host_copy(void* dst, const void* src, size_t bytes, bool device_to_host,
+                      cudaStream_t st);
+
 // Schedule of the plain / mixed tile kernels: S non-zeros per lane (tile = 32*S), a worker
 // (one warp) walks `tiles_per_worker` consecutive tiles, `warps_per_cta` workers per CTA.
 struct TileConfig {

@@ -92,3 +92,31 @@ def test_run_benchmark_after_stream_keeps_prepared_x(cuda_ok):
     assert h.run_benchmark() == 0 and h.get_y() == 0
     assert np.array_equal(y, y_ref)
     h.close()
+
+
+def test_handle_copies_pageable_and_unaligned_host_arrays(cuda_ok):
+    """prepare_mem / set_x / get_y copy pageable host arrays with a kernel where the device
+    reads pageable memory, and fall back to cudaMemcpy for buffers that are not 16-byte aligned;
+    either way y is exact on integer data, set_x takes effect, and the caller may overwrite x
+    as soon as set_x returns."""
+    a = gen.powerlaw(50_000, seed=31)
+    val = gen.uniform_int(a.nnz, 32, 10)
+    for offset in (0, 1):  # 16-byte aligned arrays, then views 8 bytes off
+        def arr(v):
+            buf = np.zeros(v.size + 2)
+            out = buf[offset:offset + v.size]
+            out[:] = v
+            return out
+        x1, x2 = arr(gen.uniform_int(a.n, 33, 10)), arr(gen.uniform_int(a.n, 34, 10))
+        y = arr(np.full(a.m, -1.0))
+        h = sp.BhsparseSpmvCuda(sp.VALUE_F64)
+        assert h.set_config(16, 4, 4, 0) == 0
+        assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, val, x1, y) == 0
+        assert h.run_benchmark() == 0 and h.get_y() == 0
+        assert np.array_equal(y, oracle.csr_serial(a.row_ptr, a.col, val, x1)), offset
+        assert h.set_x(x2) == 0
+        x2[:] = -7.0  # already read by set_x
+        assert h.run_benchmark() == 0 and h.get_y() == 0
+        assert np.array_equal(y, oracle.csr_serial(a.row_ptr, a.col, val,
+                                                   gen.uniform_int(a.n, 34, 10))), offset
+        h.close()
