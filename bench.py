@@ -486,9 +486,9 @@ def run_ours(args) -> None:
                                          "step, pinned host x / y"},
                     "per_call_pageable": {"value": round(e2e_pg_value, 2), "unit": UNIT,
                                           "path": "the same per-call sequence on pageable "
-                                                  "(malloc'd) host x / y, copied by a kernel "
-                                                  "where the device reads and writes pageable "
-                                                  "memory"}},
+                                                  "(malloc'd) host x / y: x read by a copy "
+                                                  "kernel where the device reads pageable "
+                                                  "memory, y written back by cudaMemcpy"}},
             "tuning": tuning if tuning is not None else {"prepare_mem_choice": choice},
             "gpu_launches": 2 * args.steps,
             "clocks": clocks,

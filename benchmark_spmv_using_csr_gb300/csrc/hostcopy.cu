@@ -1,12 +1,13 @@
-// hostcopy.cu -- copies between device memory and pageable host memory by a kernel.
+// hostcopy.cu -- host -> device copies of pageable host memory by a kernel.
 //
-// On a Grace host the GPU reads and writes the CPU's pageable memory coherently through the
-// host's page tables (cudaDevAttrPageableMemoryAccess and
-// cudaDevAttrPageableMemoryAccessUsesHostPageTables both 1).  A copy kernel over such memory
-// moves 33.5 MB at 196 GB/s where cudaMemcpy from the same pageable buffer, staged through pinned
-// bounce buffers by the driver, reaches 160 GB/s (pinned memory: about 205 GB/s either way).  The
-// handle API uses it for the caller's arrays when they are pageable: the reference's callers pass
-// plain malloc'd arrays (spmv_cuda/main.cu:745-746).
+// On a Grace host the GPU reads the CPU's pageable memory coherently through the host's page
+// tables (cudaDevAttrPageableMemoryAccess and cudaDevAttrPageableMemoryAccessUsesHostPageTables
+// both 1).  Measured on GB300 for 33.5 MB (python -m benchmark_spmv_using_csr_gb300.probes):
+//   pageable -> device: copy kernel 197 GB/s, cudaMemcpy (staged by the driver) 168 GB/s;
+//   device -> pageable: copy kernel 168 GB/s, cudaMemcpy 182 GB/s;
+//   pinned memory: about 205 / 189 GB/s either way.
+// So the handle API reads the caller's pageable arrays with the kernel and writes y back with
+// cudaMemcpy.  The reference's callers pass plain malloc'd arrays (spmv_cuda/main.cu:745-746).
 #include <atomic>
 
 #include "internal.h"
@@ -55,10 +56,9 @@ bool is_pageable_host(const void* p) {
 cudaError_t host_copy(void* dst, const void* src, size_t bytes, bool device_to_host,
                       cudaStream_t st) {
     if (bytes == 0) return cudaSuccess;
-    const void* host = device_to_host ? dst : src;
     const bool aligned = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) &
                           15u) == 0u;
-    if (!aligned || !host_direct_access() || !is_pageable_host(host))
+    if (device_to_host || !aligned || !host_direct_access() || !is_pageable_host(src))
         return cudaMemcpyAsync(dst, src, bytes,
                                device_to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice,
                                st);

@@ -13,10 +13,11 @@ int device_sm_count();
 // min(ceil(work / threads), cap_per_sm * SMs), at least 1: the grid of a grid-stride launch
 int grid_for(long long work, int threads, int cap_per_sm);
 
-// hostcopy.cu: host <-> device copies for the handle API.  The device reads / writes pageable
-// host memory coherently where it has pageable memory access through the host's page tables
-// (Grace); host_copy then uses a copy kernel for pageable, 16-byte-aligned host buffers and
-// cudaMemcpyAsync otherwise.
+// hostcopy.cu: host <-> device copies for the handle API.  The device reads pageable host
+// memory coherently where it has pageable memory access through the host's page tables (Grace);
+// host_copy then reads pageable, 16-byte-aligned host buffers with a copy kernel (faster than
+// the driver's staged cudaMemcpy there) and uses cudaMemcpyAsync for everything else, including
+// every device -> host copy (cudaMemcpy is the faster writer).
 bool host_direct_access();
 bool is_pageable_host(const void* p);
 cudaError_t host_copy(void* dst, const void* src, size_t bytes, bool device_to_host,

@@ -7,8 +7,9 @@
 //   * through the tensor unit: cp.async.bulk.tensor.2d ... tile::gather4 (x viewed as rows of 32
 //     or 16 bytes, one-row boxes, four rows per instruction) into an NSTAGE-deep ring of
 //     128-byte-aligned shared-memory slots per warp, every mbarrier wait bounded;
-// and host <-> device copies of x's size: cudaMemcpyAsync from pinned memory against a copy
-// kernel over mapped pinned memory.  Prints one line per case.  Built and run by
+// and host <-> device copies of x's size: cudaMemcpyAsync against a copy kernel, over pinned
+// (mapped) memory and over pageable memory (the kernel only where the device reads pageable
+// memory through the host's page tables).  Prints one line per case.  Built and run by
 // `python -m benchmark_spmv_using_csr_gb300.probes`.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -318,7 +319,7 @@ int main() {
             CK(cudaEventElapsedTime(&ms, e0, e1));
             if (rep) t.push_back(ms);
         }
-        std::printf("%-36s: %6.1f GB/s\n", name, bytes / (median_ms(t) * 1e-3) / 1e9);
+        std::printf("%-38s: %6.1f GB/s\n", name, bytes / (median_ms(t) * 1e-3) / 1e9);
     };
     copy_rate([&] { CK(cudaMemcpyAsync(d_a, h_a, bytes, cudaMemcpyHostToDevice, st)); },
               "cudaMemcpyAsync host -> device");
@@ -328,6 +329,31 @@ int main() {
               "copy kernel, mapped host -> device");
     copy_rate([&] { k_copy<<<sms * 4, 512, 0, st>>>((const int4*)d_a, (int4*)m_b, bytes / 16); },
               "copy kernel, device -> mapped host");
+    // pageable (malloc'd) host memory: cudaMemcpy stages it through pinned buffers; where the
+    // device reads the host's page tables (Grace), a copy kernel reaches it directly
+    int pageable = 0, host_tables = 0;
+    CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, 0));
+    CK(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, 0));
+    void* p_a = std::malloc(bytes);
+    void* p_b = std::malloc(bytes);
+    if (p_a && p_b) {
+        std::memset(p_a, 3, bytes);
+        std::memset(p_b, 4, bytes);
+        copy_rate([&] { CK(cudaMemcpyAsync(d_a, p_a, bytes, cudaMemcpyHostToDevice, st)); },
+                  "cudaMemcpyAsync pageable -> device");
+        copy_rate([&] { CK(cudaMemcpyAsync(p_b, d_a, bytes, cudaMemcpyDeviceToHost, st)); },
+                  "cudaMemcpyAsync device -> pageable");
+        if (pageable == 1 && host_tables == 1) {
+            copy_rate([&] { k_copy<<<sms * 4, 512, 0, st>>>((const int4*)p_a, (int4*)d_a, bytes / 16); },
+                      "copy kernel, pageable -> device");
+            copy_rate([&] { k_copy<<<sms * 4, 512, 0, st>>>((const int4*)d_a, (int4*)p_b, bytes / 16); },
+                      "copy kernel, device -> pageable");
+        } else {
+            std::printf("no pageable memory access through the host's page tables\n");
+        }
+    }
+    std::free(p_a);
+    std::free(p_b);
     CK(cudaFreeHost(h_a));
     CK(cudaFreeHost(h_b));
     CK(cudaFree(d_a));

@@ -105,10 +105,10 @@ int bhsp_get_schedule_source(const bhsp_spmv* h, int* source, float* confidence)
 int bhsp_get_config(const bhsp_spmv* h, int* seg, int* tiles_per_worker, int* warps_per_cta,
                     int* stages);
 /* Replace x (host pointer, same type as in prepare_mem) without rebuilding anything; returns
- * once x has been read, so the caller may reuse its buffer.  As prepare_mem and get_y do, it
- * reads pageable host memory with a copy kernel where the device accesses pageable memory
- * through the host's page tables (a Grace host: 196 against 160 GB/s for cudaMemcpy), and
- * copies pinned memory with cudaMemcpy. */
+ * once x has been read, so the caller may reuse its buffer.  As prepare_mem does, it reads
+ * pageable host memory with a copy kernel where the device accesses pageable memory through the
+ * host's page tables (a Grace host: 197 against 168 GB/s for cudaMemcpy), and pinned memory with
+ * cudaMemcpy. */
 int bhsp_set_x(bhsp_spmv* h, const void* x);
 /* Streamed SpMVs over many right-hand sides held in host memory: y_host[i] = A x_host[i] for
  * i = 0..count-1, with the upload of x_{i+1} and the download of y_{i-1} overlapping the SpMV of
