@@ -570,8 +570,11 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
 
 // Resident warps per SM asked of the register allocator (the launch bound is that many warps
 // divided by the warps of a CTA), measured per arithmetic policy on the 27-point stencil and the
-// power-law matrix at 16, 20 and 24 warps (4-warp CTAs):
-//  * S = 8: 24 (80 registers) for every policy;
+// power-law matrix at 16 to 32 warps (4-warp CTAs):
+//  * S = 8: 24 (80 registers) for plain FP64 (28 and 32 warps spill: 11 % and 22 % slower on the
+//    power-law matrix), 32 (64 registers) for FP32 and the mixed forms' per-slot kernels (-1.4 %
+//    FP32, -2.8 % mixed FP32, -1.5 % BF16 values on the power-law matrix against 24); the mixed
+//    one-head kernels, which would spill at 64 registers, keep 24;
 //  * plain FP64 at S = 16 and 32: 16 (128 registers).  Left alone the S = 32 kernel takes 136
 //    registers and 12 warps; at 128 it does not spill and runs 13 % faster on the stencil, while
 //    20 or 24 warps spill and run 1.5-2.4x slower;
@@ -579,12 +582,12 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
 //    16) and 20 at S = 32 (-5.2 % on the stencil);
 //  * the mixed forms: 20 (mixed FP32 -3.8 % at S = 32 and -10.5 % at S = 16 on the stencil,
 //    -2.1 % at S = 16 on the power-law matrix; BF16 values -12 % at S = 16).
-template <class P, int S>
+template <class P, int S, bool OH>
 constexpr int resident_warps() {
-    if constexpr (S == 8)
-        return 24;
-    else if constexpr (std::is_same<typename P::VC, double>::value)
-        return 16;
+    if constexpr (std::is_same<typename P::VC, double>::value)
+        return S == 8 ? 24 : 16;
+    else if constexpr (S == 8)
+        return OH && !std::is_same<typename P::Acc, float>::value ? 24 : 32;
     else if constexpr (std::is_same<typename P::Acc, float>::value)
         return S == 16 ? 24 : 20;
     else
@@ -593,7 +596,7 @@ constexpr int resident_warps() {
 
 // One warp = one worker, worker = global warp index (static schedule).
 template <class P, int S, int WARPS, bool OH, bool XL2>
-__global__ void __launch_bounds__(WARPS * 32, (resident_warps<P, S>() / WARPS))
+__global__ void __launch_bounds__(WARPS * 32, (resident_warps<P, S, OH>() / WARPS))
     k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
     // Plain FP64 with the one-head form (long rows) keeps two slot -> row maps per warp where
     // they fit in 40 KB (all but S = 32 at 8 warps), so that the next tile's map is built half-
