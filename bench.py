@@ -758,14 +758,16 @@ def measure_batched(args) -> dict:
     """The batched workload: 512 matrices (rows log-uniform in [1e3, 2e5], mixed generators),
     FP32 storage with compensated accumulation, k right-hand sides, one persistent kernel
     replayed from a CUDA graph at the batched autotuner's pick -- against the plain FP64 form
-    launched once per matrix and right-hand side (512*k sequential plain launches).  nnz*k per
-    second, and the normwise error of a subset of matrices against the FP64 oracle."""
+    launched once per matrix and right-hand side (512*k sequential plain launches), and against
+    the plain FP64 form on the whole concatenated block-diagonal matrix at its autotuned
+    schedule (one SpMV per right-hand side).  nnz*k per second, and the normwise error of a
+    subset of matrices against the FP64 oracle."""
     import numpy as np
     import torch
 
     import benchmark_spmv_using_csr_gb300 as sp
     import oracle
-    from benchmark_spmv_using_csr_gb300 import batch, gen
+    from benchmark_spmv_using_csr_gb300 import batch, gen, tune
     mats = gen.batch_workload(512)
     nnz = sum(a.nnz for a in mats)
     mats_m, mats_n = sum(a.m for a in mats), sum(a.n for a in mats)
@@ -805,6 +807,24 @@ def measure_batched(args) -> dict:
         p[0].close()
     del plans
     torch.cuda.empty_cache()
+    # the plain FP64 form on the concatenated matrix: the same non-zeros in one SpMV
+    cat = batch.concatenate(mats)
+    rp, ci = torch.from_numpy(cat["row_ptr"]).cuda(), torch.from_numpy(cat["col"]).cuda()
+    v64 = torch.from_numpy(cat["val"]).cuda()
+    x64 = torch.from_numpy(gen.uniform(cat["n"], 1)).cuda()
+    y64 = torch.zeros(cat["m"], dtype=torch.float64, device="cuda")
+    tab, best = tune.autotune(sp.VALUE_F64, rp, ci, v64, x64, y64, warmup=1, reps=5)
+    cfg = tune.candidates()[best]
+    pc = sp.Plan(sp.VALUE_F64, cat["m"], cat["n"], rp, ci, seg=cfg[0], tiles_per_worker=cfg[1],
+                 warps_per_cta=cfg[2], stages=cfg[3])
+    ms_cat = timed(lambda: pc.execute(v64, x64, y64), 10)
+    pc.check()
+    out["plain_fp64_concatenated"] = {"ms_per_rhs": round(ms_cat, 4),
+                                      "gnnz_per_s": round(nnz / ms_cat / 1e6, 2),
+                                      "schedule": list(cfg), "launches_per_rhs": pc.launches}
+    pc.close()
+    del rp, ci, v64, x64, y64, cat
+    torch.cuda.empty_cache()
     for k in (1, 2, 4, 8):
         xh = gen.uniform(mats_n * k, 3).reshape(mats_n, k).astype(np.float32)
         xd = torch.from_numpy(xh).cuda()
@@ -826,6 +846,7 @@ def measure_batched(args) -> dict:
         info = b.info()
         out[f"k{k}"] = {"ms": round(ms, 4), "gnnz_k_per_s": round(gk, 2),
                         "vs_plain_fp64_sequential": round(ms_plain * k / ms, 2),
+                        "vs_plain_fp64_concatenated": round(ms_cat * k / ms, 2),
                         "normwise_err_vs_fp64_oracle_max": worst, "launches": info["launches"],
                         "graph": True, "schedule": tb["pick"],
                         "variant": {"one_head": info["one_head"], "x_l2_only": info["x_l2_only"]},
