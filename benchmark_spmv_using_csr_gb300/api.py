@@ -260,6 +260,15 @@ class Plan:
             raise SpmvError(rc, self.last_error)
         return sm.value, nr.value, bool(l2.value)
 
+    def set_variant(self, one_head: bool | None = None, l2_only: bool | None = None) -> None:
+        """Force the chunk form and / or the gather path (None keeps the plan's rule).  Every
+        variant gives the same y; only the speed differs."""
+        oh = -1 if one_head is None else int(bool(one_head))
+        l2 = -1 if l2_only is None else int(bool(l2_only))
+        rc = self._L.bhsp_plan_set_variant(self._p, oh, l2)
+        if rc != BHSPARSE_SUCCESS:
+            raise SpmvError(rc, "bhsp_plan_set_variant failed")
+
     @property
     def last_error(self) -> str:
         return self._L.bhsp_plan_last_error(self._p).decode()

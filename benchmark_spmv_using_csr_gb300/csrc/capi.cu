@@ -361,6 +361,14 @@ extern "C" int bhsp_plan_gather_path(const bhsp_plan* p, int* sampled, int* near
     return BHSPARSE_SUCCESS;
 }
 
+extern "C" int bhsp_plan_set_variant(bhsp_plan* p, int one_head, int l2_only) {
+    if (!p || one_head < -1 || one_head > 1 || l2_only < -1 || l2_only > 1)
+        return BHSPARSE_INVALID_ARGUMENT;
+    if (one_head >= 0) p->one_head = one_head == 1;
+    if (l2_only >= 0) p->x_l2 = l2_only == 1;
+    return BHSPARSE_SUCCESS;
+}
+
 extern "C" const char* bhsp_plan_last_error(const bhsp_plan* p) {
     return p ? p->last_error.c_str() : "null plan";
 }

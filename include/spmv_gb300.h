@@ -168,6 +168,10 @@ int bhsp_plan_chunk_form(const bhsp_plan* p, int* short_rows, int* one_head);
  * row or of the same-position entry of the previous row; *l2_only = 1 (x gathered from L2
  * only, ld.global.cg) when fewer than half do, else x goes through L1. */
 int bhsp_plan_gather_path(const bhsp_plan* p, int* sampled, int* near, int* l2_only);
+/* Overrides the kernel variant the plan's rules chose: one_head (the chunk form above) and
+ * l2_only (the gather path) = 1 or 0 to force it, -1 to keep the rule's choice.  Every variant
+ * gives the same y; only the speed differs.  Takes effect at the next bhsp_plan_execute. */
+int bhsp_plan_set_variant(bhsp_plan* p, int one_head, int l2_only);
 const char* bhsp_plan_last_error(const bhsp_plan* p);
 void bhsp_plan_destroy(bhsp_plan* p);
 
