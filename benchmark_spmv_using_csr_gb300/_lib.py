@@ -72,6 +72,7 @@ SIGNATURES = {
     "bhsp_batch_info": (c_int, [c_void_p, P_int, P_int, P_int, P_int]),
     "bhsp_batch_last_error": (c_char_p, [c_void_p]),
     "bhsp_batch_variant": (c_int, [c_void_p, P_int, P_int]),
+    "bhsp_batch_set_variant": (c_int, [c_void_p, c_int, c_int]),
     "bhsp_batch_tune_num_candidates": (c_int, []),
     "bhsp_batch_tune_candidate": (c_int, [c_int, P_int, P_int, P_int]),
     "bhsp_batch_autotune": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int,

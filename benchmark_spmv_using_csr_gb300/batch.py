@@ -107,6 +107,15 @@ class Batch:
         out.update(one_head=bool(oh.value), x_l2_only=bool(l2.value))
         return out
 
+    def set_variant(self, one_head: bool | None = None, l2_only: bool | None = None) -> None:
+        """Force the chunk form (one right-hand side only) and / or the gather path; None keeps
+        the batch's rule.  Every variant gives the same y."""
+        oh = -1 if one_head is None else int(bool(one_head))
+        l2 = -1 if l2_only is None else int(bool(l2_only))
+        rc = lib().bhsp_batch_set_variant(self._b, oh, l2)
+        if rc != 0:
+            raise RuntimeError(f"bhsp_batch_set_variant failed with status {rc}")
+
     @property
     def last_error(self) -> str:
         return lib().bhsp_batch_last_error(self._b).decode()

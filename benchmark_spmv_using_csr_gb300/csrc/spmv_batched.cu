@@ -554,6 +554,25 @@ extern "C" int bhsp_batch_variant(const bhsp_batch* b, int* one_head, int* l2_on
     return BHSPARSE_SUCCESS;
 }
 
+extern "C" int bhsp_batch_set_variant(bhsp_batch* b, int one_head, int l2_only) {
+    if (!b || one_head < -1 || one_head > 1 || l2_only < -1 || l2_only > 1 ||
+        (one_head == 1 && b->k != 1))
+        return BHSPARSE_INVALID_ARGUMENT;
+    BatchVariant v = b->var;
+    if (one_head >= 0) v.one_head = one_head == 1;
+    if (l2_only >= 0) v.x_l2 = l2_only == 1;
+    const int grid = batch_grid(b->k, b->cfg, v);
+    if (grid <= 0) return batch_cuda(b, cudaErrorInvalidConfiguration, "batch variant");
+    b->var = v;
+    b->grid = grid;
+    // the captured graph launches the previous kernel: capture again at the next execute
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    return BHSPARSE_SUCCESS;
+}
+
 // ---------------------------------------------------------------------------------------
 // Schedule tuner of the batched form
 // ---------------------------------------------------------------------------------------

@@ -222,6 +222,10 @@ int bhsp_batch_info(const bhsp_batch* b, int* ntiles, int* nworkers, int* grid, 
  * (one right-hand side and few rows shorter than a chunk), *l2_only = 1 when x is gathered from
  * L2 only (fewer than half of about 2^20 sampled columns lie near their neighbours). */
 int bhsp_batch_variant(const bhsp_batch* b, int* one_head, int* l2_only);
+/* Overrides that choice: one_head / l2_only = 1 or 0 to force, -1 to keep.  The one-head form
+ * exists for one right-hand side only (one_head = 1 with k > 1 is rejected).  Every variant
+ * gives the same y; the next bhsp_batch_execute with use_graph captures the graph again. */
+int bhsp_batch_set_variant(bhsp_batch* b, int one_head, int l2_only);
 /* The batched form's schedule tuner.  Candidates: S 8 / 16 / 32 x 1 / 2 / 4 / 8 tiles per
  * worker x 4 / 8 warps per CTA.  bhsp_batch_autotune builds the batch at every candidate and
  * times bhsp_batch_execute (graph replay; `warmup` untimed runs, then the median of `reps`

@@ -26,19 +26,34 @@ def _mats(seed, count=24, integer=False):
 @pytest.mark.parametrize("k", [1, 2, 4, 8])
 @pytest.mark.parametrize("cfg", [(16, 4, 4), (8, 1, 8), (32, 2, 4)])
 def test_batched_integer_bit_exact(cuda_ok, k, cfg):
+    """Every kernel variant (the one-head form at k = 1; L2-only gathers on and off), forced
+    with bhsp_batch_set_variant, through graph replay and direct launches."""
     import torch
     mats = _mats(7, integer=True)
     b = batch.Batch(mats, k=k, seg=cfg[0], tiles_per_worker=cfg[1], warps_per_cta=cfg[2])
     x_np = (gen.uniform_int(b.n * k, 5, 10) - 4.0).reshape(b.n, k)
     x = torch.from_numpy(x_np.astype(np.float32)).cuda()
     y = torch.full((b.m, k), float("nan"), dtype=torch.float32, device="cuda")
-    b.execute(x, y)
-    b.check()
-    yh = y.cpu().numpy().astype(np.float64)
     cat = b.cat
-    for j in range(k):
-        yr = oracle.csr_serial(cat["row_ptr"], cat["col"], cat["val"], x_np[:, j].copy())
-        np.testing.assert_array_equal(yh[:, j], yr)
+    yr = [oracle.csr_serial(cat["row_ptr"], cat["col"], cat["val"], x_np[:, j].copy())
+          for j in range(k)]
+    variants = [(None, None)] + [(oh, l2) for oh in ((False, True) if k == 1 else (False,))
+                                 for l2 in (False, True)]
+    for oh, l2 in variants:
+        b.set_variant(one_head=oh, l2_only=l2)
+        info = b.info()
+        if oh is not None:
+            assert (info["one_head"], info["x_l2_only"]) == (oh, l2)
+        for use_graph in (True, False):
+            y.fill_(float("nan"))
+            b.execute(x, y, use_graph=use_graph)
+            b.check()
+            yh = y.cpu().numpy().astype(np.float64)
+            for j in range(k):
+                np.testing.assert_array_equal(yh[:, j], yr[j], err_msg=str((oh, l2, use_graph, j)))
+    if k > 1:
+        with pytest.raises(RuntimeError):
+            b.set_variant(one_head=True)
     b.close()
 
 
