@@ -695,17 +695,22 @@ def measure_comparators(args, a, x, ystar) -> dict:
 
 
 def cpu_openmp(a, x, B, seconds: float) -> dict:
-    """The reference's OpenMP CSR loop (spmv_cuda/main.cu:377-393, C port) at its 4 threads
-    (main.cu:370) and at every host thread, whole-matrix passes for about `seconds` each."""
+    """The reference's OpenMP CSR loop (spmv_cuda/main.cu:377-393) at its 4 threads
+    (main.cu:370) and at every host thread, whole-matrix passes for about `seconds` each: the
+    reference's own loop from oracle/_ref where it was built, else the oracle's C port."""
     import numpy as np
     import oracle
-    y = np.zeros(a.m)
-    out = {}
+    ref = oracle.ref_lib() is not None
+    y = np.zeros(max(a.m, 1))
+    out = {"kind": "reference" if ref else "port"}
     for label, threads in (("threads_4", 4), ("threads_all", os.cpu_count() or 1)):
         passes = 0
         t0 = time.perf_counter()
         while True:
-            oracle.csr_omp(a.row_ptr, a.col, a.val, x, threads, y=y)
+            if ref:
+                oracle.ref_omp(a.row_ptr, a.col, a.val, x, threads, runs=1, y=y)
+            else:
+                oracle.csr_omp(a.row_ptr, a.col, a.val, x, threads, y=y)
             passes += 1
             el = time.perf_counter() - t0
             if el >= seconds:
@@ -859,22 +864,30 @@ def measure_batched(args) -> dict:
 
 
 def cpu_baseline(a, x, B, seconds: float) -> dict:
-    """The reference's serial CSR loop (spmv_cuda/main.cu:755-761, C port) on one host core,
-    whole-matrix passes until `seconds` have elapsed."""
+    """The reference's serial CSR loop (spmv_cuda/main.cu:755-761) on one host core, whole-
+    matrix passes until `seconds` have elapsed: the reference's own loop compiled from its source
+    (oracle/_ref, kind "reference") where it was built, else the oracle's C port (kind "port")."""
     import numpy as np
     import oracle
-    y = np.zeros(a.m)
+    ref = oracle.ref_lib() is not None
+    y = np.zeros(max(a.m, 1))
     passes = 0
     t0 = time.perf_counter()
     while True:
-        oracle.csr_serial_rows(a.row_ptr, a.col, a.val, x, y, 0, a.m)
+        if ref:
+            oracle.ref_serial(a.row_ptr, a.col, a.val, x, y=y)
+        else:
+            oracle.csr_serial_rows(a.row_ptr, a.col, a.val, x, y, 0, a.m)
         passes += 1
         el = time.perf_counter() - t0
         if el >= seconds:
             break
-    return {"value": round(B * passes / el / 1e9, 3), "unit": UNIT, "cores": 1, "kind": "port",
+    what = ("the reference's own loop compiled from its source in oracle/_ref" if ref
+            else "C port in oracle/")
+    return {"value": round(B * passes / el / 1e9, 3), "unit": UNIT, "cores": 1,
+            "kind": "reference" if ref else "port",
             "sample": f"{passes} whole-matrix passes of the serial CSR loop (spmv_cuda/main.cu:"
-                      f"755-761, C port in oracle/) in {el:.1f} s on one host core"}
+                      f"755-761, {what}) in {el:.1f} s on one host core"}
 
 
 def main() -> None:

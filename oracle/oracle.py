@@ -300,8 +300,9 @@ def ref_calibrate(row_ptr, stage: KernelStage):
     return y[:m], y[m]
 
 
-def ref_serial(row_ptr, col, val, x) -> np.ndarray:
-    """The reference's own serial CSR loop (spmv_cuda/main.cu:753-762, compiled from its source)."""
+def ref_serial(row_ptr, col, val, x, y=None) -> np.ndarray:
+    """The reference's own serial CSR loop (spmv_cuda/main.cu:753-762, compiled from its source),
+    into ``y`` when given (contiguous, of val's type, at least max(m, 1) entries)."""
     L = ref_lib()
     rp, ci = _c(row_ptr, np.int32), _c(col, np.int32)
     m = rp.size - 1
@@ -309,7 +310,9 @@ def ref_serial(row_ptr, col, val, x) -> np.ndarray:
     vp = _f32p if vt == np.float32 else _f64p
     fn = L.ref_serial_f32 if vt == np.float32 else L.ref_serial_f64
     v, xx = _c(val, vt), _c(x, vt)
-    y = np.zeros(max(m, 1), vt)
+    if y is None:
+        y = np.zeros(max(m, 1), vt)
+    assert y.dtype == vt and y.flags.c_contiguous and y.size >= max(m, 1)
     fn(m, _p(rp, _i32p), _p(ci, _i32p), _p(v, vp), _p(xx, vp), _p(y, vp))
     return y[:m]
 

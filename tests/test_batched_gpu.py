@@ -24,10 +24,12 @@ def _mats(seed, count=24, integer=False):
 
 
 @pytest.mark.parametrize("k", [1, 2, 4, 8])
-@pytest.mark.parametrize("cfg", [(16, 4, 4), (8, 1, 8), (32, 2, 4)])
+@pytest.mark.parametrize("cfg", [(16, 4, 4), (8, 1, 8), (32, 2, 4), (16, 2, 8), (8, 3, 4),
+                                 (32, 1, 8)])
 def test_batched_integer_bit_exact(cuda_ok, k, cfg):
-    """Every kernel variant (the one-head form at k = 1; L2-only gathers on and off), forced
-    with bhsp_batch_set_variant, through graph replay and direct launches."""
+    """Every persistent kernel: each non-zeros-per-lane and warps-per-CTA pair, and every kernel
+    variant (the one-head form at k = 1; L2-only gathers on and off) forced with
+    bhsp_batch_set_variant, through graph replay and direct launches."""
     import torch
     mats = _mats(7, integer=True)
     b = batch.Batch(mats, k=k, seg=cfg[0], tiles_per_worker=cfg[1], warps_per_cta=cfg[2])
