@@ -120,3 +120,44 @@ def test_handle_copies_pageable_and_unaligned_host_arrays(cuda_ok):
         assert np.array_equal(y, oracle.csr_serial(a.row_ptr, a.col, val,
                                                    gen.uniform_int(a.n, 34, 10))), offset
         h.close()
+
+
+def test_handles_in_concurrent_host_threads(cuda_ok):
+    """Handles are independent: eight host threads, each with its own handle (the four value
+    types, two matrices), prepare, run and read back at the same time; every y is exact."""
+    import threading
+    mats = [gen.powerlaw(30000, seed=41), gen.stencil3d(24, 24, 24, seed=42)]
+    jobs = [(vt, i) for vt in (sp.VALUE_F64, sp.VALUE_F32, sp.VALUE_MIXED_F32,
+                               sp.VALUE_MIXED_BF16) for i in range(2)]
+    results, errors = {}, []
+
+    def work(vt, i):
+        try:
+            a = mats[i]
+            dt = sp.host_dtype(vt)
+            val = (gen.uniform_int(a.nnz, 50 + i, 10) - 4.0).astype(dt)
+            x = (gen.uniform_int(a.n, 60 + i, 10) - 4.0).astype(dt)
+            y = np.full(a.m, np.nan, dt)
+            h = sp.BhsparseSpmvCuda(vt)
+            assert h.init_platform() == 0, h.last_error
+            assert h.prepare_mem(a.m, a.n, a.nnz, a.row_ptr, a.col, val, x, y) == 0, h.last_error
+            for _ in range(3):
+                assert h.run_benchmark() == 0, h.last_error
+            assert h.get_y() == 0, h.last_error
+            h.free_mem()
+            h.close()
+            results[(vt, i)] = (y.astype(np.float64), val.astype(np.float64),
+                                x.astype(np.float64))
+        except Exception as e:  # reported on the main thread
+            errors.append((vt, i, repr(e)))
+
+    threads = [threading.Thread(target=work, args=j) for j in jobs]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for (vt, i), (y, val, x) in results.items():
+        a = mats[i]
+        yr = oracle.csr_serial(a.row_ptr, a.col, val, x)
+        assert np.array_equal(y, yr), (vt, i)
