@@ -12,7 +12,8 @@ matrix out of L2; steps are timed with CUDA events.
     python -m benchmark_spmv_using_csr_gb300.run_case --batched K [--config S TPW WARPS 0]
 
 runs the 512-matrix batched workload instead (FP32 storage, K = 1, 2, 4 or 8 right-hand sides),
-one graph replay per step, at the given schedule or the batch's default.
+one graph replay per step, at the given schedule or the batch's default; with --one-matrix, a
+batch of the --workload matrix alone (its multi-right-hand-side SpMV).
 """
 from __future__ import annotations
 
@@ -36,6 +37,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--batched", type=int, choices=(1, 2, 4, 8), default=None,
                     help="the 512-matrix batched workload at this many right-hand sides")
+    ap.add_argument("--one-matrix", action="store_true",
+                    help="with --batched: a batch of the --workload matrix alone")
     args = ap.parse_args()
     if args.batched:
         run_batched(args)
@@ -78,7 +81,7 @@ def run_batched(args) -> None:
 
     from benchmark_spmv_using_csr_gb300 import batch, gen
     k = args.batched
-    mats = gen.batch_workload(512)
+    mats = [gen.WORKLOADS[args.workload]()] if args.one_matrix else gen.batch_workload(512)
     cfg = args.config[:3] if args.config else (0, 0, 0)
     b = batch.Batch(mats, k=k, seg=cfg[0], tiles_per_worker=cfg[1], warps_per_cta=cfg[2])
     x = torch.from_numpy(gen.uniform(b.n * k, 3).reshape(b.n, k).astype(np.float32)).cuda()

@@ -116,7 +116,8 @@ def test_batched_autotune_pick_is_correct_and_no_slower(cuda_ok, tmp_path, k):
     b, t = batch.tuned(mats, k, x, y, cache=cache, reps=3)
     cands = batch.tune_candidates()
     ms = np.array([t["table_ms"][",".join(map(str, c))] for c in cands])
-    assert np.all(ms > 0) and tuple(t["pick"]) == cands[int(np.argmin(ms))]
+    # the pick is a fastest entry (the table is rounded to 0.1 us, so ties can hide the order)
+    assert np.all(ms > 0) and ms[cands.index(tuple(t["pick"]))] == ms.min()
     dflt = (32 if k == 4 else 16, 4, 4)
     assert dflt in cands and ms.min() <= ms[cands.index(dflt)]
     y.fill_(float("nan"))
@@ -148,3 +149,23 @@ def test_batched_variant_follows_the_columns(cuda_ok):
         info = b.info()
         assert not info["x_l2_only"] and info["one_head"] == (k == 1)
         b.close()
+
+
+@pytest.mark.parametrize("k", [2, 8])
+def test_one_matrix_many_right_hand_sides(cuda_ok, k):
+    """A batch of one matrix is the multi-RHS SpMV of that matrix: k right-hand sides in one
+    persistent launch, exact on integer data."""
+    import torch
+    a = gen.stencil3d(30, 30, 30, seed=3)
+    a.val = gen.uniform_int(a.nnz, 8, 10) - 4.0
+    b = batch.Batch([a], k=k)
+    x_np = (gen.uniform_int(a.n * k, 9, 10) - 4.0).reshape(a.n, k)
+    x = torch.from_numpy(x_np.astype(np.float32)).cuda()
+    y = torch.full((a.m, k), float("nan"), dtype=torch.float32, device="cuda")
+    b.execute(x, y)
+    b.check()
+    yh = y.cpu().numpy().astype(np.float64)
+    for j in range(k):
+        np.testing.assert_array_equal(yh[:, j], oracle.csr_serial(a.row_ptr, a.col, a.val,
+                                                                  x_np[:, j].copy()))
+    b.close()
