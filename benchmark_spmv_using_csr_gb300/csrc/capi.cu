@@ -86,6 +86,7 @@ struct bhsp_plan {
     int* rec_row = nullptr;
     void* rec_val = nullptr;
     uint32_t* err = nullptr;  // device error word
+    int* ticket = nullptr;    // [2] the persistent tile kernel's work queue
     int short_rows = 0;     // non-empty rows shorter than one chunk of a lane's slots
     bool one_head = false;  // the tile kernels take the one-head chunk form
     int x_sampled = 0, x_near = 0;  // sampled non-zeros, those with a near column
@@ -116,10 +117,12 @@ static void plan_release(bhsp_plan* p) {
     cudaFree(p->rec_row);
     cudaFree(p->rec_val);
     cudaFree(p->err);
+    cudaFree(p->ticket);
     p->tile_ptr = nullptr;
     p->rec_row = nullptr;
     p->rec_val = nullptr;
     p->err = nullptr;
+    p->ticket = nullptr;
 }
 
 static int validate_on_device(const int* row_ptr, const int* col, int m, int n, int nnz,
@@ -165,6 +168,8 @@ static int plan_build(bhsp_plan* p, cudaStream_t st) {
     PLAN_CUDA(p, cudaMalloc(&p->rec_val, 8 * (size_t)(p->nworkers > 0 ? p->nworkers : 1)));
     PLAN_CUDA(p, cudaMalloc(&p->err, sizeof(uint32_t)));
     PLAN_CUDA(p, cudaMemsetAsync(p->err, 0, sizeof(uint32_t), st));
+    PLAN_CUDA(p, cudaMalloc(&p->ticket, 2 * sizeof(int)));
+    PLAN_CUDA(p, cudaMemsetAsync(p->ticket, 0, 2 * sizeof(int), st));
     PLAN_CUDA(p, launch_partition(p->row_ptr, p->m, p->nnz, tile, p->tile_ptr, st));
     // The kernel variant, from two counts made on the device and read back once:
     //  - the chunk form: rows shorter than the plain / mixed kernels' chunk width (scalar x
@@ -213,6 +218,7 @@ static int plan_execute(bhsp_plan* p, const void* val, const void* x, void* y, c
             a.phase = phase;
             a.one_head = p->one_head;
             a.x_l2 = p->x_l2;
+            a.ticket = p->ticket;
             e = p->vt == BHSP_VALUE_F64 ? launch_plain_f64(a, p->cfg, st) : launch_plain_f32(a, p->cfg, st);
             break;
         }
@@ -234,6 +240,7 @@ static int plan_execute(bhsp_plan* p, const void* val, const void* x, void* y, c
             a.phase = phase;
             a.one_head = p->one_head;
             a.x_l2 = p->x_l2;
+            a.ticket = p->ticket;
             e = launch_mixed(a, p->cfg, st);
             break;
         }

@@ -73,6 +73,7 @@ struct PlainLaunch {
     int phase;  // bit 0: tile kernel, bit 1: calibration kernel
     bool one_head = false;  // the plan's choice of the one-head chunk form
     bool x_l2 = false;      // the plan's choice of L2-only x gathers
+    int* ticket = nullptr;  // [2] the persistent kernel's work queue, zero between launches
 };
 cudaError_t launch_plain_f64(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_plain_f32(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
@@ -95,6 +96,7 @@ struct MixedLaunch {
     int phase;  // bit 0: tile kernel, bit 1: calibration kernel
     bool one_head = false;  // the plan's choice of the one-head chunk form
     bool x_l2 = false;      // the plan's choice of L2-only x gathers
+    int* ticket = nullptr;  // [2] the persistent kernel's work queue, zero between launches
 };
 cudaError_t launch_mixed(const MixedLaunch& a, const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_mixed_bf16(const MixedLaunch& a, const TileConfig& cfg, cudaStream_t st);

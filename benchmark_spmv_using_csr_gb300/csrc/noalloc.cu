@@ -22,7 +22,7 @@ std::mutex g_mu;
 void* g_scratch_addr[64] = {};
 
 struct Layout {
-    size_t err, tile_ptr, rec_row, rec_val, total;
+    size_t err, ticket, tile_ptr, rec_row, rec_val, total;
 };
 
 size_t up256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -42,6 +42,7 @@ Layout layout_for(int nnz, const TileConfig& c) {
     const size_t nw = (nt + c.tiles_per_worker - 1) / c.tiles_per_worker;
     Layout L;
     L.err = 0;
+    L.ticket = 8;  // two ints beside the error word
     L.tile_ptr = 256;
     L.rec_row = up256(L.tile_ptr + 4 * (nt + 1));
     L.rec_val = up256(L.rec_row + 4 * (nw > 0 ? nw : 1));
@@ -93,9 +94,11 @@ extern "C" int bhsp_spmv_f64_noalloc(const int* d_row_ptr, const int* d_col_idx,
             return BHSPARSE_CUDA_ERROR;
         if (h) return BHSPARSE_INVALID_CSR;
     }
-    // the array keeps the previous call's contents: the error word must start at zero
-    // (tile_ptr is rewritten in full by the partition, and every worker writes its record)
-    if (cudaMemsetAsync(err, 0, sizeof(uint32_t), st) != cudaSuccess) return BHSPARSE_CUDA_ERROR;
+    // the array keeps the previous call's contents: the error word and the tile kernel's work
+    // queue must start at zero (tile_ptr is rewritten in full by the partition, and every
+    // worker writes its record); one write covers both
+    if (cudaMemsetAsync(err, 0, L.ticket + 2 * sizeof(int), st) != cudaSuccess)
+        return BHSPARSE_CUDA_ERROR;
     if (launch_partition(d_row_ptr, m, nnz, 32 * cfg.seg, tile_ptr, st) != cudaSuccess)
         return BHSPARSE_CUDA_ERROR;
     PlainLaunch a;
@@ -112,6 +115,7 @@ extern "C" int bhsp_spmv_f64_noalloc(const int* d_row_ptr, const int* d_col_idx,
     a.n = n;
     a.nnz = nnz;
     a.phase = 3;
+    a.ticket = reinterpret_cast<int*>(base + L.ticket);
     if (launch_plain_f64(a, cfg, st) != cudaSuccess) return BHSPARSE_CUDA_ERROR;
     if (cudaMemcpyAsync(&h, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)

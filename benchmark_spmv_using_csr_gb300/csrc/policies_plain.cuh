@@ -73,6 +73,7 @@ inline cudaError_t launch_plain_any(const PlainLaunch& l, const TileConfig& cfg,
     a.phase = l.phase;
     a.one_head = l.one_head;
     a.x_l2 = l.x_l2;
+    a.ticket = l.ticket;
     return launch_tiles_any<P>(a, cfg, st);
 }
 

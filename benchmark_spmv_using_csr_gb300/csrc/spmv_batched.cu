@@ -9,8 +9,8 @@
 // the per-matrix tile counts are its segments.  A persistent kernel sized to the GPU's resident
 // capacity hands out workers (consecutive tile ranges) from a global atomic ticket, so the
 // uneven matrices load-balance over the SMs; the calibration kernel then adds the carry
-// records.  The ticket reset, the persistent kernel and the calibration are captured once in a
-// CUDA graph and replayed by every call.
+// records.  The persistent kernel and the calibration are captured once in a CUDA graph and
+// replayed by every call (the kernel leaves its ticket at zero for the next launch).
 #include <algorithm>
 #include <cstdio>
 #include <string>
@@ -210,12 +210,10 @@ constexpr auto persistent_kernel() {
 
 template <int K, int S, int WARPS, bool OH, bool XL2>
 static cudaError_t enqueue_batched(const TileArgs<PolMixedK<K>>& a, int tpw, int nworkers,
-                                   int ntiles, int* ticket, int grid, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(int), st);
-    if (e != cudaSuccess) return e;
+                                   int ntiles, int grid, cudaStream_t st) {
     if (nworkers > 0)
         persistent_kernel<K, S, WARPS, OH, XL2>()<<<grid, WARPS * 32, 0, st>>>(a, tpw, nworkers,
-                                                                               ntiles, ticket);
+                                                                               ntiles);
     const int cb = grid_for(nworkers, 256, 8);
     k_calibrate<PolMixedK<K>><<<cb, 256, 0, st>>>(a.rec_row, a.rec_val, nworkers, a.y, a.tile_ptr,
                                                   a.m, a.err);
@@ -268,9 +266,10 @@ static cudaError_t enqueue_k(const BatchLaunch& l, int tpw, int grid, cudaStream
     a.n = l.n;
     a.nnz = l.nnz;
     a.phase = 3;
+    a.ticket = l.ticket;
     const int nt = num_tiles(l.nnz, 32 * S);
     const int nw = (nt + tpw - 1) / tpw;
-    return enqueue_batched<K, S, WARPS, OH, XL2>(a, tpw, nw, nt, l.ticket, grid, st);
+    return enqueue_batched<K, S, WARPS, OH, XL2>(a, tpw, nw, nt, grid, st);
 }
 
 // dispatch over the variant (one-head form for k = 1 only, L2-only gathers), then S and warps
@@ -439,8 +438,9 @@ extern "C" int bhsp_batch_create(bhsp_batch** out, int count, int m_total, int n
     if (e == cudaSuccess) e = cudaMalloc(&b->rec_row, sizeof(int) * nw);
     if (e == cudaSuccess) e = cudaMalloc(&b->rec_val, sizeof(double) * k * nw);
     if (e == cudaSuccess) e = cudaMalloc(&b->err, sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&b->ticket, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->ticket, 2 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemsetAsync(b->err, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->ticket, 0, 2 * sizeof(int), st);
     if (e == cudaSuccess) e = launch_partition(d_row_ptr, m_total, nnz_total, 32 * c.seg, b->tile_ptr, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
@@ -484,7 +484,7 @@ extern "C" int bhsp_batch_execute(bhsp_batch* b, const float* d_val, const float
         return e == cudaSuccess ? BHSPARSE_SUCCESS : batch_cuda(b, e, "batched launch");
     }
     if (!b->exec || b->g_val != d_val || b->g_x != d_x || b->g_y != d_y) {
-        // (re)capture the ticket reset, the persistent kernel and the calibration
+        // (re)capture the persistent kernel and the calibration
         if (b->exec) cudaGraphExecDestroy(b->exec);
         if (b->graph) cudaGraphDestroy(b->graph);
         b->exec = nullptr;

@@ -22,8 +22,9 @@
 //    no host fix-up;
 //  * a tile without any row head keeps its partial per lane across tiles and folds it only
 //    when the row ends (one butterfly per long row instead of one per tile);
-//  * a worker (one warp) walks tiles_per_worker consecutive tiles with its carry in
-//    registers.  The row it starts inside of (the reference's synchronizer entry,
+//  * a worker is tiles_per_worker consecutive tiles, walked by one warp with its carry in
+//    registers; a matrix larger than one wave of workers runs a persistent kernel whose warps
+//    take workers from a global ticket, a smaller one a warp per worker.  The row it starts inside of (the reference's synchronizer entry,
 //    kernels_cuda.h:243-247) is the only value it cannot write itself; it goes to a
 //    per-worker carry record that k_calibrate adds in worker order after the main kernel
 //    (replacing the host loop of bhsparse_spmv_cuda.h:170-173).  Every other row is
@@ -61,6 +62,9 @@ struct TileArgs {
     bool one_head = false;
     // launcher choice, made at plan time: x gathers from L2 only (columns without locality)
     bool x_l2 = false;
+    // the persistent kernel's work queue: [0] the next worker, [1] warps done; zero before a
+    // launch, and zero again after it (the last warp to finish resets both)
+    int* ticket = nullptr;
 };
 
 // ---- shuffles for the accumulator types ----
@@ -594,16 +598,21 @@ constexpr int resident_warps() {
         return 20;
 }
 
+// Plain FP64 with the one-head form (long rows) keeps two slot -> row maps per warp where they
+// fit in 40 KB (all but S = 32 at 8 warps), so that the next tile's map is built half-way through
+// this tile's chunk loop: +1.4 % on the 27-point stencil at (32, 4, 4).  The per-slot form builds
+// it after the loop: half-way cost the power-law matrix 5-9 %.
+template <class P, int S, int WARPS, bool OH>
+constexpr bool two_maps() {
+    return OH && std::is_same<typename P::VC, double>::value && sizeof(typename P::Acc) == 8 &&
+           WARPS * 2 * 32 * S * 4 <= 40 * 1024;
+}
+
 // One warp = one worker, worker = global warp index (static schedule).
 template <class P, int S, int WARPS, bool OH, bool XL2>
 __global__ void __launch_bounds__(WARPS * 32, (resident_warps<P, S, OH>() / WARPS))
     k_tiles(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
-    // Plain FP64 with the one-head form (long rows) keeps two slot -> row maps per warp where
-    // they fit in 40 KB (all but S = 32 at 8 warps), so that the next tile's map is built half-
-    // way through this tile's chunk loop: +1.4 % on the 27-point stencil at (32, 4, 4).  The
-    // per-slot form builds it after the loop: half-way cost the power-law matrix 5-9 %.
-    constexpr bool MID = OH && std::is_same<typename P::VC, double>::value &&
-                         sizeof(typename P::Acc) == 8 && WARPS * 2 * 32 * S * 4 <= 40 * 1024;
+    constexpr bool MID = two_maps<P, S, WARPS, OH>();
     __shared__ uint32_t s_words[WARPS][32];
     __shared__ int s_rowof[WARPS][(MID ? 2 : 1) * 32 * S];
     // the calibration kernel may be scheduled now; it waits for this grid's completion itself
@@ -614,38 +623,56 @@ __global__ void __launch_bounds__(WARPS * 32, (resident_warps<P, S, OH>() / WARP
     tile_worker<P, S, OH, MID, XL2>(a, worker, tpw, ntiles, s_words[warp], s_rowof[warp]);
 }
 
-// Persistent schedule: a grid sized to the GPU's resident capacity; each warp takes the next
-// worker index from a global ticket until none is left (the global tile work queue of the
-// batched form: workers are consecutive tile ranges, so the ticket walks the tiles in order).
-// The persistent loop: each warp takes the next worker index from the ticket until none is left.
-template <class P, int S, bool OH, bool XL2>
+// Persistent tile kernels: a grid of at most the GPU's resident capacity in which each warp takes
+// the next worker (tiles_per_worker consecutive tiles) from a global ticket until none is left, so
+// that a warp that drew cheap tiles takes more of them; the static grid keeps each CTA's slot until
+// its slowest warp is done.  After its last draw a warp counts itself done, and the grid's last
+// warp puts the ticket back to zero, ready for the next launch on the stream (no reset launch or
+// graph node is needed; one plan or batch runs one SpMV at a time).  The loop stays this simple on
+// purpose: drawing the next worker at the start of the current one (to hide the atomic's round
+// trip) or a branch for grids of one wave raised the register count from 80 to 90-96 at S = 16 and
+// cost more than either saved.
+template <class P, int S, bool OH, bool MID, bool XL2>
 __device__ __forceinline__ void persistent_workers(const TileArgs<P>& a, int tpw, int nworkers,
-                                                   int ntiles, int* ticket, uint32_t* s_words_w,
-                                                   int* rowof) {
+                                                   int ntiles, uint32_t* s_words_w, int* rowof) {
     const int lane = threadIdx.x & 31;
+    int* const ticket = a.ticket;
     for (;;) {
         int w = 0;
         if (lane == 0) w = atomicAdd(ticket, 1);
         w = __shfl_sync(SPMV_FULL_MASK, w, 0);
         if (w >= nworkers) break;
-        if (w < 0) {  // cannot happen with a ticket reset to 0 before the launch
+        if (w < 0) {  // cannot happen with the ticket at zero before the launch
             if (lane == 0) atomicOr(a.err, ERR_QUEUE);
             break;
         }
-        tile_worker<P, S, OH, false, XL2>(a, w, tpw, ntiles, s_words_w, rowof);
+        tile_worker<P, S, OH, MID, XL2>(a, w, tpw, ntiles, s_words_w, rowof);
         __syncwarp();
+    }
+    if (lane == 0) {
+        __threadfence();  // this warp's last draw comes before its count
+        const int warps = (int)(gridDim.x * (blockDim.x >> 5));
+        if (atomicAdd(ticket + 1, 1) == warps - 1) {  // every warp has drawn for the last time
+            atomicExch(ticket, 0);
+            atomicExch(ticket + 1, 0);
+        }
     }
 }
 
-// OH / XL2: the plan's chunk form and x gather path, as for k_tiles (fixed per batch)
+
+// No register target: without a minimum-blocks launch bound the register allocator gives the
+// persistent kernels 62-90 registers (116-122 for plain FP64 at S = 16 and 32).
 template <class P, int S, int WARPS, bool OH, bool XL2>
 __global__ void __launch_bounds__(WARPS * 32)
-    k_tiles_persistent(TileArgs<P> a, int tpw, int nworkers, int ntiles, int* ticket) {
+    k_tiles_persistent(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
+    constexpr bool MID = two_maps<P, S, WARPS, OH>();
     __shared__ uint32_t s_words[WARPS][32];
-    __shared__ int s_rowof[WARPS][32 * S];
+    __shared__ int s_rowof[WARPS][(MID ? 2 : 1) * 32 * S];
+    // the calibration kernel may be scheduled now; it waits for this grid's completion itself
+    asm volatile("griddepcontrol.launch_dependents;");
     const int warp = threadIdx.x >> 5;
-    persistent_workers<P, S, OH, XL2>(a, tpw, nworkers, ntiles, ticket, s_words[warp],
-                                      s_rowof[warp]);
+    persistent_workers<P, S, OH, MID, XL2>(a, tpw, nworkers, ntiles, s_words[warp],
+                                           s_rowof[warp]);
 }
 
 // The same with 16 resident warps per SM asked of the register allocator (128 registers), for
@@ -655,12 +682,49 @@ __global__ void __launch_bounds__(WARPS * 32)
 // cost one right-hand side 3-14 %.
 template <class P, int S, int WARPS, bool OH, bool XL2>
 __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
-    k_tiles_persistent_capped(TileArgs<P> a, int tpw, int nworkers, int ntiles, int* ticket) {
+    k_tiles_persistent_capped(TileArgs<P> a, int tpw, int nworkers, int ntiles) {
     __shared__ uint32_t s_words[WARPS][32];
     __shared__ int s_rowof[WARPS][32 * S];
+    asm volatile("griddepcontrol.launch_dependents;");
     const int warp = threadIdx.x >> 5;
-    persistent_workers<P, S, OH, XL2>(a, tpw, nworkers, ntiles, ticket, s_words[warp],
-                                      s_rowof[warp]);
+    persistent_workers<P, S, OH, false, XL2>(a, tpw, nworkers, ntiles, s_words[warp],
+                                             s_rowof[warp]);
+}
+
+// CTAs per SM of a kernel, from the occupancy calculator (at least 1)
+template <class K>
+int ctas_per_sm(K kernel, int threads) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, 0) != cudaSuccess) b = 0;
+    return b > 0 ? b : 1;
+}
+
+// The tile kernel launch.  The persistent kernel on the GPU's resident capacity, except
+//  * when one wave of the static grid (a warp per worker) holds every worker: a small matrix,
+//    where the ticket's atomics would cost 2-4 us of a 10-20 us SpMV;
+//  * for plain FP64 in the one-head form (long rows), which is bound by GB300's FP64 pipe: the
+//    ticket's round trip between a warp's workers leaves the pipe idle, and the static grid was
+//    1.5 % faster at the best schedules on the 27-point stencil (3.8 % at (32, 4, 4)).
+// Measured on one box against the static grid everywhere, at the best of 32 schedules on 154
+// matrices of the tuner's dataset: 4.2 % (FP64), 1.2 % (FP32), 2.4 % (mixed FP32) and 1.8 %
+// (mixed BF16) faster on average above 50 us and on a par below 20 us; the power-law matrix
+// 2.5 % (FP64), the 27-point stencil 4.6 % (FP32) and 10 % (mixed FP32) faster.
+template <class P, int S, int WARPS, bool OH, bool XL2>
+void launch_tile_kernel(const TileArgs<P>& a, int tpw, int nworkers, int ntiles, cudaStream_t st) {
+    static const int static_per_sm = ctas_per_sm(k_tiles<P, S, WARPS, OH, XL2>, WARPS * 32);
+    const long long blocks = ((long long)nworkers + WARPS - 1) / WARPS;
+    const int sms = device_sm_count();
+    constexpr bool fp64_pipe_bound = OH && std::is_same<typename P::VC, double>::value;
+    if constexpr (!fp64_pipe_bound) {
+        if (blocks > (long long)sms * static_per_sm) {
+            static const int persistent_per_sm =
+                ctas_per_sm(k_tiles_persistent<P, S, WARPS, OH, XL2>, WARPS * 32);
+            k_tiles_persistent<P, S, WARPS, OH, XL2>
+                <<<sms * persistent_per_sm, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+            return;
+        }
+    }
+    k_tiles<P, S, WARPS, OH, XL2><<<(int)blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
 }
 
 // Exchange of any carry-record type between lanes (as 32-bit words).
@@ -762,19 +826,19 @@ template <class P, int S, int WARPS>
 cudaError_t launch_tiles_t(const TileArgs<P>& a, int tpw, int nworkers, int ntiles,
                            cudaStream_t st) {
     if (nworkers > 0 && (a.phase & 1)) {
-        const int blocks = (nworkers + WARPS - 1) / WARPS;
+        if (!a.ticket) return cudaErrorInvalidValue;
         if constexpr (sizeof(typename P::Acc) <= 8) {  // scalar accumulators: either form
             // chunk form x gather path, both fixed by the plan
             if (a.one_head && a.x_l2)
-                k_tiles<P, S, WARPS, true, true><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+                launch_tile_kernel<P, S, WARPS, true, true>(a, tpw, nworkers, ntiles, st);
             else if (a.one_head)
-                k_tiles<P, S, WARPS, true, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+                launch_tile_kernel<P, S, WARPS, true, false>(a, tpw, nworkers, ntiles, st);
             else if (a.x_l2)
-                k_tiles<P, S, WARPS, false, true><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+                launch_tile_kernel<P, S, WARPS, false, true>(a, tpw, nworkers, ntiles, st);
             else
-                k_tiles<P, S, WARPS, false, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+                launch_tile_kernel<P, S, WARPS, false, false>(a, tpw, nworkers, ntiles, st);
         } else {
-            k_tiles<P, S, WARPS, false, false><<<blocks, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+            launch_tile_kernel<P, S, WARPS, false, false>(a, tpw, nworkers, ntiles, st);
         }
     }
     if (a.phase & 2) {

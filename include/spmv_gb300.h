@@ -148,7 +148,9 @@ int bhsp_plan_create(bhsp_plan** out, int value_type, int m, int n, int nnz,
                      int warps_per_cta, int stages, void* stream);
 /* y = A.x, enqueued on `stream`.  d_val in the storage type of value_type (double, float,
  * float, __nv_bfloat16), 32-byte aligned; d_x / d_y in the x/y type (double for F64, float
- * otherwise). */
+ * otherwise).  A plan runs one SpMV at a time: its tile kernel's work queue and carry records
+ * are the plan's own, so calls on one plan must follow each other on one stream (or be ordered
+ * by events); separate plans run concurrently. */
 int bhsp_plan_execute(bhsp_plan* p, const void* d_val, const void* d_x, void* d_y, void* stream);
 /* One phase of bhsp_plan_execute (1 = tile kernel, 2 = calibration, 3 = both). */
 int bhsp_plan_execute_phase(bhsp_plan* p, const void* d_val, const void* d_x, void* d_y,
@@ -210,7 +212,7 @@ int bhsp_batch_create(bhsp_batch** out, int count, int m_total, int n_total, int
                       const int* d_row_ptr, const int* d_col_idx, int k, int seg,
                       int tiles_per_worker, int warps_per_cta, void* stream);
 /* y = A.x for all matrices and right-hand sides, enqueued on `stream`.  use_graph != 0 replays a
- * CUDA graph of the ticket reset, the persistent kernel and the calibration (captured on the
+ * CUDA graph of the persistent kernel and the calibration (captured on the
  * first call and again whenever the buffers change); use_graph == 0 launches them directly.
  * d_val 32-byte aligned, d_x / d_y aligned to 4*k bytes. */
 int bhsp_batch_execute(bhsp_batch* b, const float* d_val, const float* d_x, float* d_y,
