@@ -476,7 +476,8 @@ def run_ours(args) -> None:
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic, "peak_kind": f"{peak_kind} (hbm_gbs copy, burst)",
-                         "kernel": "k_tiles<PolF64> (tile kernel alone)"},
+                         "kernel": "FP64 tile kernel alone (k_tiles_persistent<PolF64> above one "
+                                   "wave of workers, else k_tiles<PolF64>)"},
             "e2e": {"value": round(e2e_value, 2), "unit": UNIT,
                     "h2d_bytes_per_step": a.n * 8, "d2h_bytes_per_step": a.m * 8,
                     "path": "bhsp_run_stream over the K steps' pinned host x / y (upload of "
