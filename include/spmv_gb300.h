@@ -332,8 +332,8 @@ void bhsp_mlp_destroy(bhsp_mlp* m);
  * real-time loops that cannot afford cudaMalloc / cudaFree (both may synchronise the whole
  * device), or processes whose device footprint must not grow after start-up.  All buffers are
  * the caller's device pointers (d_val and d_col_idx 32-byte aligned); the kernels' scratch
- * (tile partition, carry records, error word) lives in the fixed array above, so the call
- * performs no cudaMalloc, cudaFree or other allocating routine.
+ * (tile partition, carry records, error word, the tile kernel's work queue) lives in the fixed
+ * array above, so the call performs no cudaMalloc, cudaFree or other allocating routine.
  *   - The first call on each device looks up the array's device address (with that device
  *     current) and caches it for the rest of the process; make that first call before any
  *     stream capture.  The cached address does not survive a reset of the device's primary
