@@ -57,6 +57,7 @@ SIGNATURES = {
     "bhsp_plan_chunk_form": (c_int, [c_void_p, P_int, P_int]),
     "bhsp_plan_gather_path": (c_int, [c_void_p, P_int, P_int, P_int]),
     "bhsp_plan_set_variant": (c_int, [c_void_p, c_int, c_int]),
+    "bhsp_plan_set_grid": (c_int, [c_void_p, c_int]),
     "bhsp_plan_last_error": (c_char_p, [c_void_p]),
     "bhsp_plan_destroy": (None, [c_void_p]),
     # partition primitives

@@ -269,6 +269,13 @@ class Plan:
         if rc != BHSPARSE_SUCCESS:
             raise SpmvError(rc, "bhsp_plan_set_variant failed")
 
+    def set_grid(self, persistent: bool | None = None) -> None:
+        """Force the persistent (True) or the static (False) tile-kernel grid; None keeps the
+        rule.  Same y either way."""
+        rc = self._L.bhsp_plan_set_grid(self._p, -1 if persistent is None else int(bool(persistent)))
+        if rc != BHSPARSE_SUCCESS:
+            raise SpmvError(rc, "bhsp_plan_set_grid failed")
+
     @property
     def last_error(self) -> str:
         return self._L.bhsp_plan_last_error(self._p).decode()

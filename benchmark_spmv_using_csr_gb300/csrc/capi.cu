@@ -87,6 +87,7 @@ struct bhsp_plan {
     void* rec_val = nullptr;
     uint32_t* err = nullptr;  // device error word
     int* ticket = nullptr;    // [2] the persistent tile kernel's work queue
+    int grid_mode = -1;       // the tile kernel's grid: -1 by rule, 0 static, 1 persistent
     int short_rows = 0;     // non-empty rows shorter than one chunk of a lane's slots
     bool one_head = false;  // the tile kernels take the one-head chunk form
     int x_sampled = 0, x_near = 0;  // sampled non-zeros, those with a near column
@@ -219,6 +220,7 @@ static int plan_execute(bhsp_plan* p, const void* val, const void* x, void* y, c
             a.one_head = p->one_head;
             a.x_l2 = p->x_l2;
             a.ticket = p->ticket;
+            a.grid_mode = p->grid_mode;
             e = p->vt == BHSP_VALUE_F64 ? launch_plain_f64(a, p->cfg, st) : launch_plain_f32(a, p->cfg, st);
             break;
         }
@@ -241,6 +243,7 @@ static int plan_execute(bhsp_plan* p, const void* val, const void* x, void* y, c
             a.one_head = p->one_head;
             a.x_l2 = p->x_l2;
             a.ticket = p->ticket;
+            a.grid_mode = p->grid_mode;
             e = launch_mixed(a, p->cfg, st);
             break;
         }
@@ -373,6 +376,12 @@ extern "C" int bhsp_plan_set_variant(bhsp_plan* p, int one_head, int l2_only) {
         return BHSPARSE_INVALID_ARGUMENT;
     if (one_head >= 0) p->one_head = one_head == 1;
     if (l2_only >= 0) p->x_l2 = l2_only == 1;
+    return BHSPARSE_SUCCESS;
+}
+
+extern "C" int bhsp_plan_set_grid(bhsp_plan* p, int persistent) {
+    if (!p || persistent < -1 || persistent > 1) return BHSPARSE_INVALID_ARGUMENT;
+    p->grid_mode = persistent;
     return BHSPARSE_SUCCESS;
 }
 

@@ -74,6 +74,7 @@ struct PlainLaunch {
     bool one_head = false;  // the plan's choice of the one-head chunk form
     bool x_l2 = false;      // the plan's choice of L2-only x gathers
     int* ticket = nullptr;  // [2] the persistent kernel's work queue, zero between launches
+    int grid_mode = -1;     // -1 the launcher's rule, 0 static grid, 1 persistent
 };
 cudaError_t launch_plain_f64(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_plain_f32(const PlainLaunch& a, const TileConfig& cfg, cudaStream_t st);
@@ -97,6 +98,7 @@ struct MixedLaunch {
     bool one_head = false;  // the plan's choice of the one-head chunk form
     bool x_l2 = false;      // the plan's choice of L2-only x gathers
     int* ticket = nullptr;  // [2] the persistent kernel's work queue, zero between launches
+    int grid_mode = -1;     // -1 the launcher's rule, 0 static grid, 1 persistent
 };
 cudaError_t launch_mixed(const MixedLaunch& a, const TileConfig& cfg, cudaStream_t st);
 cudaError_t launch_mixed_bf16(const MixedLaunch& a, const TileConfig& cfg, cudaStream_t st);

@@ -74,6 +74,7 @@ cudaError_t launch_mixed_t(const MixedLaunch& l, const TileConfig& cfg, cudaStre
     a.one_head = l.one_head;
     a.x_l2 = l.x_l2;
     a.ticket = l.ticket;
+    a.grid_mode = l.grid_mode;
     return launch_tiles_any(a, cfg, st);
 }
 

@@ -74,6 +74,7 @@ inline cudaError_t launch_plain_any(const PlainLaunch& l, const TileConfig& cfg,
     a.one_head = l.one_head;
     a.x_l2 = l.x_l2;
     a.ticket = l.ticket;
+    a.grid_mode = l.grid_mode;
     return launch_tiles_any<P>(a, cfg, st);
 }
 

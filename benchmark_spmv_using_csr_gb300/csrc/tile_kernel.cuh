@@ -65,6 +65,9 @@ struct TileArgs {
     // the persistent kernel's work queue: [0] the next worker, [1] warps done; zero before a
     // launch, and zero again after it (the last warp to finish resets both)
     int* ticket = nullptr;
+    // the tile kernel's grid: -1 by the rule below (launch_tile_kernel), 0 static (a warp per
+    // worker), 1 persistent where the variant has a persistent kernel
+    int grid_mode = -1;
 };
 
 // ---- shuffles for the accumulator types ----
@@ -716,11 +719,15 @@ void launch_tile_kernel(const TileArgs<P>& a, int tpw, int nworkers, int ntiles,
     const int sms = device_sm_count();
     constexpr bool fp64_pipe_bound = OH && std::is_same<typename P::VC, double>::value;
     if constexpr (!fp64_pipe_bound) {
-        if (blocks > (long long)sms * static_per_sm) {
+        const bool persistent = a.grid_mode >= 0 ? a.grid_mode == 1
+                                                 : blocks > (long long)sms * static_per_sm;
+        if (persistent) {
             static const int persistent_per_sm =
                 ctas_per_sm(k_tiles_persistent<P, S, WARPS, OH, XL2>, WARPS * 32);
+            const long long cap = (long long)sms * persistent_per_sm;
             k_tiles_persistent<P, S, WARPS, OH, XL2>
-                <<<sms * persistent_per_sm, WARPS * 32, 0, st>>>(a, tpw, nworkers, ntiles);
+                <<<(int)(blocks < cap ? blocks : cap), WARPS * 32, 0, st>>>(a, tpw, nworkers,
+                                                                           ntiles);
             return;
         }
     }

@@ -174,6 +174,11 @@ int bhsp_plan_gather_path(const bhsp_plan* p, int* sampled, int* near, int* l2_o
  * l2_only (the gather path) = 1 or 0 to force it, -1 to keep the rule's choice.  Every variant
  * gives the same y; only the speed differs.  Takes effect at the next bhsp_plan_execute. */
 int bhsp_plan_set_variant(bhsp_plan* p, int one_head, int l2_only);
+/* Overrides the grid of the direct-load tile kernel: 1 = the persistent kernel (warps draw
+ * workers from the plan's work queue), 0 = a static grid of one warp per worker, -1 = the rule
+ * (persistent when the workers exceed one wave of the static grid, except plain FP64 in the
+ * one-head form, which always runs the static grid and ignores 1).  Same y either way. */
+int bhsp_plan_set_grid(bhsp_plan* p, int persistent);
 const char* bhsp_plan_last_error(const bhsp_plan* p);
 void bhsp_plan_destroy(bhsp_plan* p);
 

@@ -76,6 +76,7 @@ def test_plan_queries_reject_a_null_plan():
     assert L.bhsp_plan_tiles(None, None, None, None) == sp.BHSPARSE_INVALID_ARGUMENT
     assert L.bhsp_plan_set_variant(None, 1, 0) == sp.BHSPARSE_INVALID_ARGUMENT
     assert L.bhsp_batch_set_variant(None, 0, 1) == sp.BHSPARSE_INVALID_ARGUMENT
+    assert L.bhsp_plan_set_grid(None, 1) == sp.BHSPARSE_INVALID_ARGUMENT
 
 
 def test_run_before_prepare_is_an_error():

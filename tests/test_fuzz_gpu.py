@@ -6,7 +6,8 @@ one, a single row longer than many workers, alternating empty rows (dirty tiles 
 power-law lengths, constant lengths at and around the chunk and tile sizes, far more columns
 than rows or far more rows than columns -- and integer values whose partial sums are exact in
 FP32, so every form (plain FP64 / FP32, compensated FP32 / BF16 storage) must equal the
-reference's serial CSR loop (spmv_cuda/main.cu:755-761) exactly, whatever the schedule.
+reference's serial CSR loop (spmv_cuda/main.cu:755-761) exactly, whatever the schedule, kernel
+variant and grid (persistent or static, drawn per case).
 """
 import numpy as np
 import pytest
@@ -88,6 +89,7 @@ def test_fuzz_bit_exact(cuda_ok, vt):
             continue
         oh, l2 = bool(rng.integers(0, 2)), bool(rng.integers(0, 2))
         p.set_variant(one_head=oh, l2_only=l2)
+        p.set_grid(bool(rng.integers(0, 2)))
         if vt == sp.VALUE_F64:
             vd, xt = torch.from_numpy(val).cuda(), torch.float64
         elif vt == sp.VALUE_MIXED_BF16:

@@ -3,8 +3,9 @@
 A plan picks its tile kernel by value type, schedule (non-zeros per lane, tiles per worker, warps
 per CTA, TMA stages) and variant (the one-head chunk form; x gathered from L2 only).  Its rules
 choose the variant from the matrix, so a given matrix reaches only some kernels.  These tests
-force every variant (bhsp_plan_set_variant) at every candidate schedule of the autotuner, in every
-value type, on integer-valued matrices whose partial sums are exact in FP32: every form must then
+force every variant (bhsp_plan_set_variant) and both grids of the direct kernel (persistent and
+static, bhsp_plan_set_grid) at every candidate schedule of the autotuner, in every value type, on
+integer-valued matrices whose partial sums are exact in FP32: every form must then
 equal the reference's serial CSR loop (spmv_cuda/main.cu:755-761) bit for bit.  The matrices mix
 empty rows (dirty tiles), short rows (two row heads in one lane's chunk, which sends the one-head
 form to its per-slot path), rows of 27 non-zeros, and a row longer than a worker (carry records
@@ -82,15 +83,21 @@ def test_every_schedule_and_variant_bit_exact(cuda_ok, vt, shape):
         for oh, l2 in VARIANTS:
             p.set_variant(one_head=oh, l2_only=l2)
             assert p.chunk_form()[1] == oh and p.gather_path()[2] == l2
-            yd.fill_(float("nan"))
-            p.execute(vd, xd, yd)
-            p.check()
-            y = yd[:m].cpu().double().numpy()
-            bad = int(np.count_nonzero(y != yr))
-            assert bad == 0, (shape, vt, cfg, oh, l2, bad)
-            ran += 1
+            # both grids of the direct-load kernel: these matrices fit in one wave, so the rule
+            # alone would only ever run the static one
+            for persistent in ((False, True) if cfg[3] == 0 else (None,)):
+                p.set_grid(persistent)
+                for _ in range(2):  # a second launch finds the work queue at zero again
+                    yd.fill_(float("nan"))
+                    p.execute(vd, xd, yd)
+                    p.check()
+                    y = yd[:m].cpu().double().numpy()
+                    bad = int(np.count_nonzero(y != yr))
+                    assert bad == 0, (shape, vt, cfg, oh, l2, persistent, bad)
+                ran += 1
         p.close()
-    assert ran >= 4 * 24  # every direct schedule in every variant, and the staged ones that fit
+    assert ran >= 4 * 24 * 2  # every direct schedule in every variant and both grids, and the
+    # staged ones that fit
 
 
 def test_set_variant_keeps_the_rule_with_minus_one(cuda_ok):
