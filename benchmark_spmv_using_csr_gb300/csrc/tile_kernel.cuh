@@ -575,9 +575,9 @@ __device__ __forceinline__ void tile_worker(const TileArgs<P>& a, int worker, in
     if (!rec_written && lane == 0) a.rec_row[worker] = -1;
 }
 
-// Resident warps per SM asked of the register allocator (the launch bound is that many warps
-// divided by the warps of a CTA), measured per arithmetic policy on the 27-point stencil and the
-// power-law matrix at 16 to 32 warps (4-warp CTAs):
+// Resident warps per SM asked of the register allocator by the static-grid kernel k_tiles (the
+// launch bound is that many warps divided by the warps of a CTA), measured per arithmetic policy
+// on the 27-point stencil and the power-law matrix at 16 to 32 warps (4-warp CTAs):
 //  * S = 8: 24 (80 registers) for plain FP64 (28 and 32 warps spill: 11 % and 22 % slower on the
 //    power-law matrix), 32 (64 registers) for FP32 and the mixed forms' per-slot kernels (-1.4 %
 //    FP32, -2.8 % mixed FP32, -1.5 % BF16 values on the power-law matrix against 24); the mixed
