@@ -33,10 +33,14 @@ def _noalloc(rp, ci, val, x, y, m, n, nnz, validate=0):
         ctypes.c_void_p(y.data_ptr()), m, n, nnz, validate, ctypes.c_void_p(stream))
 
 
-@pytest.mark.parametrize("kind", ["powerlaw", "stencil27"])
+@pytest.mark.parametrize("kind", ["powerlaw", "stencil27", "powerlaw_large"])
 def test_noalloc_matches_plan_on_two_calls(cuda_ok, kind):
+    """powerlaw_large (about 21 M non-zeros) has more workers than one wave, so its tile kernel
+    is the persistent one, with the work queue in the fixed scratch."""
     import torch
-    a = gen.powerlaw(300_000, seed=21) if kind == "powerlaw" else gen.stencil3d(40, 37, 33, seed=22)
+    a = {"powerlaw": lambda: gen.powerlaw(300_000, seed=21),
+         "stencil27": lambda: gen.stencil3d(40, 37, 33, seed=22),
+         "powerlaw_large": lambda: gen.powerlaw(1_500_000, seed=24)}[kind]()
     rp, ci = torch.from_numpy(a.row_ptr).cuda(), torch.from_numpy(a.col).cuda()
     val = torch.from_numpy(a.val).cuda()
     plan = sp.Plan(sp.VALUE_F64, a.m, a.n, rp, ci)
