@@ -22,10 +22,11 @@ Metric: SpMV HBM GB/s on the algorithmic bytes B = nnz*(s_val+4) + (m+1)*4 + n*s
   probe's rate (323 G sectors/s), the unit that binds on that matrix.
 * ``roofline``: the tile kernel alone (launched on its own between CUDA events, L2 flushed
   before each) against the measured HBM copy bandwidth.
-* ``cpu_baseline``: the reference's serial CSR loop (spmv_cuda/main.cu:755-761, a port in
-  oracle/) on one host core over whole-matrix passes.
-* ``--impl reference``: the reference's OpenMP CSR loop (spmv_cuda/main.cu:377-393, same
-  port) on all host cores, same workload / metric.
+* ``cpu_baseline``: the reference's serial CSR loop (spmv_cuda/main.cu:755-761) on one host
+  core over whole-matrix passes, and its OpenMP loop at 4 and all threads: the reference's own
+  loops compiled from its source (oracle/_ref) where they were built, else the ports in oracle/.
+* ``--impl reference``: the reference's OpenMP CSR loop (spmv_cuda/main.cu:377-393, its own
+  code from oracle/_ref, else the port) on all host cores, same workload / metric.
 """
 from __future__ import annotations
 
